@@ -1,0 +1,232 @@
+// blas1.cu -- HBM-bound helpers of the DTensor API: batched transpose, axpy,
+// scal, row extraction and deterministic whole-buffer reductions.
+#include <cfloat>
+#include "common.cuh"
+
+namespace gbla {
+
+// ---------------------------------------------------------------- transpose
+// One 32x32 tile per block, staged through shared memory (padded to avoid
+// bank conflicts) so both the read of A and the write of A^T are coalesced.
+template <typename T>
+__global__ void __launch_bounds__(256) k_transpose(int m, int n, const T *__restrict__ A, int64_t sA,
+                                                   T *__restrict__ At, int64_t sAt, int batch) {
+    __shared__ T tile[32][33];
+    const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+    for (int b = blockIdx.z; b < batch; b += gridDim.z) {
+        const T *a = A + b * sA;
+        T *at = At + b * sAt;
+        for (int jj = threadIdx.y; jj < 32; jj += 8) {
+            int i = i0 + threadIdx.x, j = j0 + jj;
+            if (i < m && j < n) tile[jj][threadIdx.x] = a[(int64_t)j * m + i];
+        }
+        __syncthreads();
+        for (int ii = threadIdx.y; ii < 32; ii += 8) {
+            int j = j0 + threadIdx.x, i = i0 + ii;  // At is n x m: element (j, i)
+            if (i < m && j < n) at[(int64_t)i * n + j] = tile[threadIdx.x][ii];
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+static gbla_status transpose(int m, int n, const T *A, int64_t sA, T *At, int64_t sAt, int batch,
+                             cudaStream_t st) {
+    if (m < 0 || n < 0 || batch < 0) return GBLA_INVALID_VALUE;
+    if ((int64_t)m * n == 0 || batch == 0) return GBLA_SUCCESS;
+    if (!A || !At || sA < (int64_t)m * n || sAt < (int64_t)m * n) return GBLA_INVALID_VALUE;
+    dim3 grid((n + 31) / 32, (m + 31) / 32, batch < 65535 ? batch : 65535);
+    k_transpose<T><<<grid, dim3(32, 8), 0, st>>>(m, n, A, sA, At, sAt, batch);
+    return launch_status();
+}
+
+// --------------------------------------------------------------- axpy/scal
+template <typename T>
+__global__ void k_axpy(int64_t len, T alpha, const T *__restrict__ x, T *__restrict__ y) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = fma(alpha, x[i], y[i]);
+}
+
+template <typename T>
+__global__ void k_scal(int64_t len, T alpha, T *__restrict__ x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x)
+        x[i] *= alpha;
+}
+
+static int stream_grid(int64_t len) {
+    int64_t g = (len + 255) / 256;
+    int64_t cap = (int64_t)sm_count() * 8;
+    return (int)(g < cap ? (g > 0 ? g : 1) : cap);
+}
+
+template <typename T>
+static gbla_status axpy(int64_t len, T alpha, const T *x, T *y, cudaStream_t st) {
+    if (len < 0) return GBLA_INVALID_VALUE;
+    if (len == 0) return GBLA_SUCCESS;
+    if (!x || !y) return GBLA_INVALID_VALUE;
+    k_axpy<T><<<stream_grid(len), 256, 0, st>>>(len, alpha, x, y);
+    return launch_status();
+}
+
+template <typename T>
+static gbla_status scal(int64_t len, T alpha, T *x, cudaStream_t st) {
+    if (len < 0) return GBLA_INVALID_VALUE;
+    if (len == 0) return GBLA_SUCCESS;
+    if (!x) return GBLA_INVALID_VALUE;
+    k_scal<T><<<stream_grid(len), 256, 0, st>>>(len, alpha, x);
+    return launch_status();
+}
+
+// ---------------------------------------------------------------- copy rows
+template <typename T>
+__global__ void k_copy_rows(int m, int n, int r0, int nr, const T *__restrict__ A, T *__restrict__ out) {
+    int64_t tot = (int64_t)nr * n;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        int i = (int)(e % nr), j = (int)(e / nr);
+        out[e] = A[(int64_t)j * m + r0 + i];
+    }
+}
+
+template <typename T>
+static gbla_status copy_rows(int m, int n, int r0, int nr, const T *A, T *out, cudaStream_t st) {
+    if (m < 0 || n < 0 || nr < 0 || r0 < 0 || r0 + nr > m) return GBLA_INVALID_VALUE;
+    if ((int64_t)nr * n == 0) return GBLA_SUCCESS;
+    if (!A || !out) return GBLA_INVALID_VALUE;
+    k_copy_rows<T><<<stream_grid((int64_t)nr * n), 256, 0, st>>>(m, n, r0, nr, A, out);
+    return launch_status();
+}
+
+// --------------------------------------------------------------- reductions
+// Pass 1: a fixed number of blocks (depending only on len) each reduce a
+// grid-strided slice into one partial; pass 2: one block reduces the
+// partials in a fixed order.  The result is therefore bitwise reproducible.
+enum RedOp { RED_DOT = 0, RED_SQ = 1, RED_ABS = 2, RED_AMAX = 3, RED_AMIN = 4 };
+constexpr int RED_THREADS = 256;
+constexpr int RED_MAX_BLOCKS = 1024;
+
+template <typename T, int OP>
+__device__ __forceinline__ T red_identity() {
+    if (OP == RED_AMAX) return T(0);
+    if (OP == RED_AMIN) return T(INFINITY);
+    return T(0);
+}
+
+template <typename T, int OP>
+__device__ __forceinline__ T red_combine(T a, T b) {
+    if (OP == RED_AMAX) return a > b ? a : (b == b ? b : a);
+    if (OP == RED_AMIN) return a < b ? a : (b == b ? b : a);
+    return a + b;
+}
+
+template <typename T, int OP>
+__device__ __forceinline__ T block_reduce(T v) {
+    __shared__ T sh[RED_THREADS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = red_combine<T, OP>(v, shfl_xor(v, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < RED_THREADS / 32 ? sh[threadIdx.x] : red_identity<T, OP>();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = red_combine<T, OP>(v, shfl_xor(v, o));
+    }
+    return v;
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_pass1(int64_t len, const T *__restrict__ x,
+                                                               const T *__restrict__ y, T *partials) {
+    T acc = red_identity<T, OP>();
+    for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * RED_THREADS) {
+        T v = x[i];
+        T t;
+        if (OP == RED_DOT) t = v * y[i];
+        else if (OP == RED_SQ) t = v * v;
+        else t = v < T(0) ? -v : v;
+        acc = red_combine<T, OP>(acc, t);
+    }
+    acc = block_reduce<T, OP>(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_pass2(int nparts, const T *partials, T *result) {
+    T acc = red_identity<T, OP>();
+    for (int i = threadIdx.x; i < nparts; i += RED_THREADS) acc = red_combine<T, OP>(acc, partials[i]);
+    acc = block_reduce<T, OP>(acc);
+    if (threadIdx.x == 0) *result = (OP == RED_SQ) ? dev_sqrt<T>(acc) : acc;
+}
+
+template <typename T, int OP>
+static gbla_status reduce(int64_t len, const T *x, const T *y, T *result, void *ws, cudaStream_t st) {
+    if (len < 0 || !result || !ws) return GBLA_INVALID_VALUE;
+    if (len > 0 && (!x || (OP == RED_DOT && !y))) return GBLA_INVALID_VALUE;
+    int64_t nb = (len + RED_THREADS * 4 - 1) / (RED_THREADS * 4);
+    if (nb < 1) nb = 1;
+    if (nb > RED_MAX_BLOCKS) nb = RED_MAX_BLOCKS;
+    T *parts = reinterpret_cast<T *>(ws);
+    k_reduce_pass1<T, OP><<<(int)nb, RED_THREADS, 0, st>>>(len, x, y, parts);
+    gbla_status s = launch_status();
+    if (s != GBLA_SUCCESS) return s;
+    k_reduce_pass2<T, OP><<<1, RED_THREADS, 0, st>>>((int)nb, parts, result);
+    return launch_status();
+}
+
+}  // namespace gbla
+
+using namespace gbla;
+
+GBLA_API gbla_status gbla_stranspose_batched(int m, int n, const float *A, int64_t sA, float *At, int64_t sAt,
+                                             int batch, cudaStream_t st) {
+    return transpose<float>(m, n, A, sA, At, sAt, batch, st);
+}
+GBLA_API gbla_status gbla_dtranspose_batched(int m, int n, const double *A, int64_t sA, double *At,
+                                             int64_t sAt, int batch, cudaStream_t st) {
+    return transpose<double>(m, n, A, sA, At, sAt, batch, st);
+}
+GBLA_API gbla_status gbla_saxpy(int64_t len, float alpha, const float *x, float *y, cudaStream_t st) {
+    return axpy<float>(len, alpha, x, y, st);
+}
+GBLA_API gbla_status gbla_daxpy(int64_t len, double alpha, const double *x, double *y, cudaStream_t st) {
+    return axpy<double>(len, alpha, x, y, st);
+}
+GBLA_API gbla_status gbla_sscal(int64_t len, float alpha, float *x, cudaStream_t st) {
+    return scal<float>(len, alpha, x, st);
+}
+GBLA_API gbla_status gbla_dscal(int64_t len, double alpha, double *x, cudaStream_t st) {
+    return scal<double>(len, alpha, x, st);
+}
+GBLA_API gbla_status gbla_scopy_rows(int m, int n, int r0, int nr, const float *A, float *out, cudaStream_t st) {
+    return copy_rows<float>(m, n, r0, nr, A, out, st);
+}
+GBLA_API gbla_status gbla_dcopy_rows(int m, int n, int r0, int nr, const double *A, double *out,
+                                     cudaStream_t st) {
+    return copy_rows<double>(m, n, r0, nr, A, out, st);
+}
+GBLA_API size_t gbla_reduce_workspace_bytes(void) { return RED_MAX_BLOCKS * sizeof(double); }
+
+#define GBLA_RED(NAME, T, OP, HASY)                                                                    \
+    GBLA_API gbla_status NAME(int64_t len, const T *x, HASY T *result, void *ws, cudaStream_t st) {   \
+        return reduce<T, OP>(len, x, YARG, result, ws, st);                                            \
+    }
+#define YARG nullptr
+GBLA_RED(gbla_snrm2, float, RED_SQ, )
+GBLA_RED(gbla_dnrm2, double, RED_SQ, )
+GBLA_RED(gbla_sasum, float, RED_ABS, )
+GBLA_RED(gbla_dasum, double, RED_ABS, )
+GBLA_RED(gbla_samax, float, RED_AMAX, )
+GBLA_RED(gbla_damax, double, RED_AMAX, )
+GBLA_RED(gbla_samin, float, RED_AMIN, )
+GBLA_RED(gbla_damin, double, RED_AMIN, )
+#undef YARG
+GBLA_API gbla_status gbla_sdot(int64_t len, const float *x, const float *y, float *result, void *ws,
+                               cudaStream_t st) {
+    return reduce<float, RED_DOT>(len, x, y, result, ws, st);
+}
+GBLA_API gbla_status gbla_ddot(int64_t len, const double *x, const double *y, double *result, void *ws,
+                               cudaStream_t st) {
+    return reduce<double, RED_DOT>(len, x, y, result, ws, st);
+}

@@ -1,0 +1,370 @@
+// chol.cu -- batched Cholesky factor / solve / fused factor+solve+refine.
+//
+// Two kernel shapes, chosen by n:
+//  * n <= 32  : "lane-row" kernel.  A group of NB lanes (NB = 8, 16 or 32)
+//               owns one matrix, lane r holds row r in registers; the
+//               right-looking factorisation and both triangular solves run
+//               with warp shuffles only (no shared memory, no barriers).
+//               32/NB matrices per warp, 4 warps per block.
+//  * n <= 128+: "CTA" kernel.  One block (8 warps) per matrix, the matrix in
+//               shared memory with an odd leading dimension; one barrier per
+//               column (the owner warp of column k+1 finishes it while the
+//               other warps still update), each right-hand side solved by
+//               its own warp with shuffle broadcasts.
+// Refinement (posv) recomputes r = b - A x from the lower triangle of the
+// original A, which stays untouched in global memory until L is stored.
+#include "common.cuh"
+
+namespace gbla {
+
+enum CholMode { CH_FACTOR = 1, CH_SOLVE = 2 };
+
+// residual accumulation type of the refinement
+template <typename T> struct ResT { using type = double; };
+
+// ------------------------------------------------------------ lane-row kernel
+template <typename T, int NB>
+__device__ __forceinline__ void lr_factor(T (&a)[NB], T &dinv, int &fail, int n, int r) {
+#pragma unroll
+    for (int k = 0; k < NB; k++) {
+        if (k < n) {
+            T d = shfl(a[k], k, NB);
+            if (!(d > T(0)) && fail == 0) fail = k + 1;
+            T l = dev_sqrt<T>(d);
+            T il = T(1) / l;
+            if (r == k) { a[k] = l; dinv = il; }
+            else if (r > k) a[k] *= il;
+#pragma unroll
+            for (int j = k + 1; j < NB; j++) {
+                if (j < n) {
+                    T ljk = shfl(a[k], j, NB);
+                    if (r >= j) a[j] -= a[k] * ljk;
+                }
+            }
+        }
+    }
+}
+
+// Solve L L^T x = b for one right-hand side held one row per lane.
+template <typename T, int NB>
+__device__ __forceinline__ T lr_solve(const T (&a)[NB], T dinv, T b, int n, int r) {
+#pragma unroll
+    for (int k = 0; k < NB; k++) {
+        if (k < n) {
+            if (r == k) b *= dinv;
+            T yk = shfl(b, k, NB);
+            if (r > k) b -= a[k] * yk;
+        }
+    }
+#pragma unroll
+    for (int k = NB - 1; k >= 0; k--) {
+        if (k < n) {
+            T part = (r > k && r < n) ? a[k] * b : T(0);
+            T s = group_sum(part, NB);
+            if (r == k) b = (b - s) * dinv;
+        }
+    }
+    return b;
+}
+
+// y_r = (A x)_r for symmetric A given by its lower triangle in global memory.
+template <typename T, int NB, typename R>
+__device__ __forceinline__ R lr_symv_lower(const T *__restrict__ a, int n, int r, bool rowok, R x) {
+    R acc = R(0);
+#pragma unroll 4
+    for (int j = 0; j < n; j++) {
+        R xj = shfl(x, j, NB);
+        R aij = (rowok && r >= j) ? R(a[(int64_t)j * n + r]) : R(0);
+        acc += aij * xj;                           // lower part incl. diagonal
+        R up = (r > j) ? aij * x : R(0);           // A(j, r) x_r for r > j
+        up = group_sum(up, NB);
+        if (r == j) acc += up;
+    }
+    return acc;
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(128, 1) k_chol_lanerow(int n, int nrhs, T *__restrict__ A, int64_t sA,
+                                                      T *__restrict__ B, int64_t sB, int *__restrict__ info,
+                                                      int mode, int refine, int batch) {
+    using R = typename ResT<T>::type;
+    constexpr int GPW = 32 / NB;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane / NB, r = lane % NB;
+    const int64_t mat = ((int64_t)blockIdx.x * 4 + warp) * GPW + g;
+    const bool act = mat < batch;
+    const bool rowok = act && r < n;
+    T *a_g = A + (act ? mat : 0) * sA;
+
+    T a[NB];
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+        bool ld = rowok && j < n && j <= r;
+        a[j] = ld ? a_g[(int64_t)j * n + r] : T(r == j ? 1 : 0);
+    }
+    T dinv = T(1);
+    int fail = 0;
+    if (mode & CH_FACTOR) {
+        lr_factor<T, NB>(a, dinv, fail, n, r);
+        if (act && r == 0 && info) info[mat] = fail;
+    } else {
+#pragma unroll
+        for (int j = 0; j < NB; j++)
+            if (j == r) dinv = T(1) / a[j];
+    }
+    if (mode & CH_SOLVE) {
+        T *b_g = B + (act ? mat : 0) * sB;
+        for (int c = 0; c < nrhs; c++) {
+            T b = rowok ? b_g[(int64_t)c * n + r] : T(0);
+            T x = lr_solve<T, NB>(a, dinv, b, n, r);
+            if ((mode & CH_FACTOR) && refine > 0) {
+                R xr = R(x);
+                for (int it = 0; it < refine; it++) {
+                    R ax = lr_symv_lower<T, NB, R>(a_g, n, r, rowok, xr);
+                    T res = rowok ? T(R(b) - ax) : T(0);
+                    T d = lr_solve<T, NB>(a, dinv, res, n, r);
+                    xr += R(d);
+                }
+                x = T(xr);
+            }
+            if (rowok) b_g[(int64_t)c * n + r] = x;
+        }
+    }
+    if ((mode & CH_FACTOR) && rowok) {
+#pragma unroll
+        for (int j = 0; j < NB; j++)
+            if (j < n && j <= r) a_g[(int64_t)j * n + r] = a[j];
+    }
+}
+
+// ------------------------------------------------------------------ CTA kernel
+constexpr int CTA_THREADS = 256;
+constexpr int CTA_WARPS = CTA_THREADS / 32;
+constexpr int CTA_RHS_CHUNK = CTA_WARPS;  // one warp per right-hand side
+
+__host__ __device__ inline int cta_ld(int n) { return n | 1; }
+
+template <typename T>
+__host__ __device__ inline size_t cta_smem_bytes(int n) {
+    int ld = cta_ld(n);
+    return sizeof(T) * ((size_t)n * ld + (size_t)n * CTA_RHS_CHUNK + n) + 16;
+}
+
+// Solve L L^T x = b for the column x (length n, shared memory) with one warp.
+template <typename T>
+__device__ __forceinline__ void cta_solve_col(const T *__restrict__ a, int ld, const T *__restrict__ dinv,
+                                              T *__restrict__ x, int n, int lane) {
+    for (int k = 0; k < n; k++) {
+        T xk = x[k] * dinv[k];
+        for (int i = k + 1 + lane; i < n; i += 32) x[i] -= a[(int64_t)k * ld + i] * xk;
+        __syncwarp();
+        if (lane == 0) x[k] = xk;
+        __syncwarp();
+    }
+    for (int k = n - 1; k >= 0; k--) {
+        T xk = x[k] * dinv[k];
+        for (int i = lane; i < k; i += 32) x[i] -= a[(int64_t)i * ld + k] * xk;  // L(k, i)
+        __syncwarp();
+        if (lane == 0) x[k] = xk;
+        __syncwarp();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CTA_THREADS, 1) k_chol_cta(int n, int nrhs, T *__restrict__ A, int64_t sA,
+                                                          T *__restrict__ B, int64_t sB, int *__restrict__ info,
+                                                          int mode, int refine, int batch) {
+    using R = typename ResT<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *a = reinterpret_cast<T *>(smem_raw);
+    const int ld = cta_ld(n);
+    T *xs = a + (size_t)n * ld;
+    T *dinv = xs + (size_t)n * CTA_RHS_CHUNK;
+    __shared__ int s_fail;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    for (int64_t mat = blockIdx.x; mat < batch; mat += gridDim.x) {
+        T *a_g = A + mat * sA;
+        // lower triangle -> shared memory (warp per column, lanes along rows)
+        for (int j = warp; j < n; j += CTA_WARPS)
+            for (int i = j + lane; i < n; i += 32) a[(int64_t)j * ld + i] = a_g[(int64_t)j * n + i];
+        if (threadIdx.x == 0) s_fail = 0;
+        __syncthreads();
+
+        if (mode & CH_FACTOR) {
+            for (int k = 0; k < n; k++) {
+                if (warp == k % CTA_WARPS) {
+                    __syncwarp();
+                    T d = a[(int64_t)k * ld + k];
+                    if (!(d > T(0)) && lane == 0 && s_fail == 0) s_fail = k + 1;
+                    T l = dev_sqrt<T>(d);
+                    T il = T(1) / l;
+                    for (int i = k + 1 + lane; i < n; i += 32) a[(int64_t)k * ld + i] *= il;
+                    if (lane == 0) { a[(int64_t)k * ld + k] = l; dinv[k] = il; }
+                }
+                __syncthreads();
+                // update own columns j > k (column k+1 first: it is next step's pivot)
+                int j0 = k + 1 + ((warp - (k + 1) % CTA_WARPS) + CTA_WARPS) % CTA_WARPS;
+                for (int j = j0; j < n; j += CTA_WARPS) {
+                    T ljk = a[(int64_t)k * ld + j];
+                    for (int i = j + lane; i < n; i += 32) a[(int64_t)j * ld + i] -= a[(int64_t)k * ld + i] * ljk;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0 && info) info[mat] = s_fail;
+        } else {
+            for (int k = threadIdx.x; k < n; k += CTA_THREADS) dinv[k] = T(1) / a[(int64_t)k * ld + k];
+            __syncthreads();
+        }
+
+        if (mode & CH_SOLVE) {
+            T *b_g = B + mat * sB;
+            for (int c0 = 0; c0 < nrhs; c0 += CTA_RHS_CHUNK) {
+                int c = c0 + warp;
+                if (c < nrhs) {
+                    T *x = xs + (size_t)warp * n;
+                    for (int i = lane; i < n; i += 32) x[i] = b_g[(int64_t)c * n + i];
+                    __syncwarp();
+                    cta_solve_col<T>(a, ld, dinv, x, n, lane);
+                    if ((mode & CH_FACTOR) && refine > 0) {
+                        // x is kept in T; corrections come from an R-precision residual.
+                        for (int it = 0; it < refine; it++) {
+                            // r = b - A x (A symmetric, lower triangle of the original in global)
+                            // each lane accumulates rows i = lane + 32 s
+                            R acc[4] = {R(0), R(0), R(0), R(0)};
+                            for (int j = 0; j < n; j++) {
+                                R xj = R(x[j]);
+                                R up = R(0);
+#pragma unroll
+                                for (int s = 0; s < 4; s++) {
+                                    int i = lane + 32 * s;
+                                    if (i < n && i >= j) {
+                                        R aij = R(a_g[(int64_t)j * n + i]);
+                                        acc[s] += aij * xj;
+                                        if (i > j) up += aij * R(x[i]);
+                                    }
+                                }
+                                up = warp_sum(up);
+#pragma unroll
+                                for (int s = 0; s < 4; s++)
+                                    if (lane == (j & 31) && (j >> 5) == s) acc[s] += up;
+                            }
+                            __syncwarp();
+                            T *d = x;  // reuse: store residual in a scratch column after x
+                            T rv[4];
+#pragma unroll
+                            for (int s = 0; s < 4; s++) {
+                                int i = lane + 32 * s;
+                                rv[s] = i < n ? T(R(b_g[(int64_t)c * n + i]) - acc[s]) : T(0);
+                            }
+                            // keep x in registers while the residual is solved in place
+                            T xv[4];
+#pragma unroll
+                            for (int s = 0; s < 4; s++) {
+                                int i = lane + 32 * s;
+                                xv[s] = i < n ? x[i] : T(0);
+                            }
+                            __syncwarp();
+#pragma unroll
+                            for (int s = 0; s < 4; s++) {
+                                int i = lane + 32 * s;
+                                if (i < n) d[i] = rv[s];
+                            }
+                            __syncwarp();
+                            cta_solve_col<T>(a, ld, dinv, d, n, lane);
+#pragma unroll
+                            for (int s = 0; s < 4; s++) {
+                                int i = lane + 32 * s;
+                                if (i < n) x[i] = xv[s] + d[i];
+                            }
+                            __syncwarp();
+                        }
+                    }
+                    for (int i = lane; i < n; i += 32) b_g[(int64_t)c * n + i] = x[i];
+                }
+            }
+        }
+        __syncthreads();
+        if (mode & CH_FACTOR) {
+            for (int j = warp; j < n; j += CTA_WARPS)
+                for (int i = j + lane; i < n; i += 32) a_g[(int64_t)j * n + i] = a[(int64_t)j * ld + i];
+        }
+        __syncthreads();
+    }
+}
+
+static int max_cta_n(size_t elem) {
+    // largest n whose working set fits the 227 KB opt-in shared memory
+    int n = 32;
+    while (true) {
+        size_t b = elem * ((size_t)(n + 1) * cta_ld(n + 1) + (size_t)(n + 1) * CTA_RHS_CHUNK + (n + 1)) + 16;
+        if (b > 227 * 1024) break;
+        n++;
+    }
+    return n;
+}
+
+template <typename T>
+static gbla_status chol_launch(int n, int nrhs, T *A, int64_t sA, T *B, int64_t sB, int *info, int mode,
+                               int refine, int batch, cudaStream_t st) {
+    if (n < 0 || batch < 0 || nrhs < 0 || refine < 0) return GBLA_INVALID_VALUE;
+    if (batch == 0 || n == 0) return GBLA_SUCCESS;
+    if (!A || sA < (int64_t)n * n) return GBLA_INVALID_VALUE;
+    if ((mode & CH_SOLVE) && (!B || sB < (int64_t)n * nrhs)) return GBLA_INVALID_VALUE;
+    if ((mode & CH_SOLVE) && nrhs == 0 && !(mode & CH_FACTOR)) return GBLA_SUCCESS;
+    if (n > 128 && n > max_cta_n(sizeof(T))) return GBLA_NOT_SUPPORTED;
+    // refinement reads rows lane + 32 s for s < 4 in the CTA kernel
+    if (refine > 0 && n > 128) return GBLA_NOT_SUPPORTED;
+    if (n <= 32) {
+        int nb = n <= 8 ? 8 : (n <= 16 ? 16 : 32);
+        int mpb = 4 * (32 / nb);
+        int64_t grid = (batch + mpb - 1) / mpb;
+        if (grid > 0x7fffffff) return GBLA_INVALID_VALUE;
+        if (nb == 8)
+            k_chol_lanerow<T, 8><<<(unsigned)grid, 128, 0, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+        else if (nb == 16)
+            k_chol_lanerow<T, 16><<<(unsigned)grid, 128, 0, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+        else
+            k_chol_lanerow<T, 32><<<(unsigned)grid, 128, 0, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+        return launch_status();
+    }
+    size_t smem = cta_smem_bytes<T>(n);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_chol_cta<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return from_cuda(e);
+    }
+    int per_sm = (int)((228 * 1024) / (smem + 1024));
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 8) per_sm = 8;
+    int64_t grid = (int64_t)sm_count() * per_sm;
+    if (grid > batch) grid = batch;
+    k_chol_cta<T><<<(unsigned)grid, CTA_THREADS, smem, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+    return launch_status();
+}
+
+}  // namespace gbla
+
+using namespace gbla;
+
+GBLA_API gbla_status gbla_spotrf_batched(int n, float *A, int64_t sA, int *info, int batch, cudaStream_t st) {
+    return chol_launch<float>(n, 0, A, sA, nullptr, 0, info, CH_FACTOR, 0, batch, st);
+}
+GBLA_API gbla_status gbla_dpotrf_batched(int n, double *A, int64_t sA, int *info, int batch, cudaStream_t st) {
+    return chol_launch<double>(n, 0, A, sA, nullptr, 0, info, CH_FACTOR, 0, batch, st);
+}
+GBLA_API gbla_status gbla_spotrs_batched(int n, int nrhs, const float *L, int64_t sL, float *B, int64_t sB,
+                                         int batch, cudaStream_t st) {
+    return chol_launch<float>(n, nrhs, const_cast<float *>(L), sL, B, sB, nullptr, CH_SOLVE, 0, batch, st);
+}
+GBLA_API gbla_status gbla_dpotrs_batched(int n, int nrhs, const double *L, int64_t sL, double *B, int64_t sB,
+                                         int batch, cudaStream_t st) {
+    return chol_launch<double>(n, nrhs, const_cast<double *>(L), sL, B, sB, nullptr, CH_SOLVE, 0, batch, st);
+}
+GBLA_API gbla_status gbla_sposv_batched(int n, int nrhs, float *A, int64_t sA, float *B, int64_t sB, int *info,
+                                        int refine, int batch, cudaStream_t st) {
+    return chol_launch<float>(n, nrhs, A, sA, B, sB, info, CH_FACTOR | CH_SOLVE, refine, batch, st);
+}
+GBLA_API gbla_status gbla_dposv_batched(int n, int nrhs, double *A, int64_t sA, double *B, int64_t sB,
+                                        int *info, int refine, int batch, cudaStream_t st) {
+    return chol_launch<double>(n, nrhs, A, sA, B, sB, info, CH_FACTOR | CH_SOLVE, refine, batch, st);
+}

@@ -1,0 +1,162 @@
+/*
+ * gbla.h -- C ABI of libgbla.so, the GB300 (sm_103a) batched small-matrix
+ * linear-algebra library behind the GPUtils-compatible tensor.cuh.
+ *
+ * Every entry point replaces one cuBLAS / cuSOLVER call (or a host loop of
+ * them) made by GPUtils' include/tensor.cuh; the comment above each one cites
+ * the reference call site it replaces.  The functions take plain device
+ * pointers, sizes and batch strides (in elements), never pointer arrays:
+ * DTensor keeps its matrices back to back, so base pointer + stride covers
+ * every case the reference builds, including axis-2 slices.
+ *
+ * Conventions
+ *  - Matrices are column-major with leading dimension = number of rows.
+ *  - All calls are asynchronous on the given stream and allocate nothing;
+ *    reductions that need scratch take a caller-provided workspace.
+ *  - Errors are returned as gbla_status; nothing is thrown or printed and the
+ *    process is never terminated.  Numerical failures are reported per matrix
+ *    through device `info` arrays with cuSOLVER's meaning (0 = success).
+ *  - Pointer arguments documented as "nullable" may be NULL.
+ */
+#ifndef GBLA_H
+#define GBLA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without requiring the CUDA headers (same typedef as CUDA's). */
+struct CUstream_st;
+typedef struct CUstream_st *cudaStream_t;
+
+typedef enum gbla_status {
+    GBLA_SUCCESS = 0,
+    GBLA_INVALID_VALUE = 1,    /* a size, stride or pointer argument is invalid */
+    GBLA_NOT_SUPPORTED = 2,    /* valid request outside what this build implements */
+    GBLA_CUDA_ERROR = 3,       /* a CUDA runtime call or kernel launch failed */
+    GBLA_WORKSPACE_TOO_SMALL = 4
+} gbla_status;
+
+/* Precision schedule for single-precision GEMM. */
+typedef enum gbla_gemm_mode {
+    GBLA_GEMM_AUTO = 0,   /* tensor-core split path where the shape allows it, else FP32 FFMA */
+    GBLA_GEMM_FP32 = 1,   /* plain FP32 fused multiply-add on the CUDA cores */
+    GBLA_GEMM_BF16X6 = 2  /* operands split into three BF16 terms, six tcgen05 products,
+                             FP32 accumulation in tensor memory */
+} gbla_gemm_mode;
+
+/* Human-readable name of a status code. */
+const char *gbla_status_string(gbla_status s);
+/* Library version, major*10000 + minor*100 + patch. */
+int gbla_version(void);
+/* Last CUDA runtime error code seen by the library (0 if none). */
+int gbla_last_cuda_error(void);
+/* Bit mask of device-side bounded waits that ran out since the previous call
+ * (bit 0: tensor-core GEMM mbarrier wait).  Reading clears it; -1 if the
+ * flags could not be read.  Synchronises the current device. */
+int gbla_device_error_flags(void);
+
+/* ------------------------------------------------------------------ GEMM */
+/* C_i <- alpha * A_i * B_i + beta * C_i for i < batch.  A_i is m x k,
+ * B_i is k x n, C_i is m x n.  C must not overlap A or B.
+ * Replaces cublas<t>gemmBatched / cublas<t>gemm in DTensor::addAB
+ * (include/tensor.cuh:1286-1338). */
+gbla_status gbla_sgemm_batched(int m, int n, int k, float alpha, const float *A, int64_t strideA,
+                               const float *B, int64_t strideB, float beta, float *C,
+                               int64_t strideC, int batch, gbla_gemm_mode mode, cudaStream_t stream);
+gbla_status gbla_dgemm_batched(int m, int n, int k, double alpha, const double *A, int64_t strideA,
+                               const double *B, int64_t strideB, double beta, double *C,
+                               int64_t strideC, int batch, cudaStream_t stream);
+
+/* -------------------------------------------------------------- Cholesky */
+/* In-place lower Cholesky A_i = L_i L_i^T of n x n matrices.  The strictly
+ * upper triangle is not touched.  info[i] = 0 on success, j if the leading
+ * minor of order j is not positive definite.
+ * Replaces cusolverDn<t>potrfBatched (include/tensor.cuh:2135-2159) and
+ * cusolverDn<t>potrf (include/tensor.cuh:1742-1761).  n <= 128. */
+gbla_status gbla_spotrf_batched(int n, float *A, int64_t strideA, int *info, int batch,
+                                cudaStream_t stream);
+gbla_status gbla_dpotrf_batched(int n, double *A, int64_t strideA, int *info, int batch,
+                                cudaStream_t stream);
+
+/* Solve L_i L_i^T X_i = B_i in place (B_i is n x nrhs) with the lower factor
+ * in L_i.  Replaces cusolverDn<t>potrsBatched (include/tensor.cuh:2161-2197)
+ * and cusolverDn<t>potrs (include/tensor.cuh:1763-1783); nrhs >= 1 (the
+ * reference supports nrhs = 1 only).  n <= 128. */
+gbla_status gbla_spotrs_batched(int n, int nrhs, const float *L, int64_t strideL, float *B,
+                                int64_t strideB, int batch, cudaStream_t stream);
+gbla_status gbla_dpotrs_batched(int n, int nrhs, const double *L, int64_t strideL, double *B,
+                                int64_t strideB, int batch, cudaStream_t stream);
+
+/* Fused factor + solve + iterative refinement: one pass that leaves L_i in
+ * A_i and X_i in B_i.  refine_iters refinement steps use an extended-
+ * precision residual B_i - A_i X_i computed from the original A_i.  Equivalent
+ * to CholeskyBatchFactoriser::factorise() followed by solve()
+ * (include/tensor.cuh:2135-2197) for any nrhs.  n <= 128. */
+gbla_status gbla_sposv_batched(int n, int nrhs, float *A, int64_t strideA, float *B,
+                               int64_t strideB, int *info, int refine_iters, int batch,
+                               cudaStream_t stream);
+gbla_status gbla_dposv_batched(int n, int nrhs, double *A, int64_t strideA, double *B,
+                               int64_t strideB, int *info, int refine_iters, int batch,
+                               cudaStream_t stream);
+
+/* ------------------------------------------------------- level-1 / copy */
+/* Per-matrix transpose: At_i (n x m) = A_i^T (A_i is m x n).
+ * Replaces the host loop of cublas<t>geam in DTensor::tr (include/tensor.cuh:1167-1197). */
+gbla_status gbla_stranspose_batched(int m, int n, const float *A, int64_t strideA, float *At,
+                                    int64_t strideAt, int batch, cudaStream_t stream);
+gbla_status gbla_dtranspose_batched(int m, int n, const double *A, int64_t strideA, double *At,
+                                    int64_t strideAt, int batch, cudaStream_t stream);
+
+/* y <- alpha x + y over len elements.  Replaces cublas<t>axpy in
+ * DTensor::operator+= / -= (include/tensor.cuh:1239-1276). */
+gbla_status gbla_saxpy(int64_t len, float alpha, const float *x, float *y, cudaStream_t stream);
+gbla_status gbla_daxpy(int64_t len, double alpha, const double *x, double *y, cudaStream_t stream);
+
+/* x <- alpha x.  Replaces cublas<t>scal in DTensor::operator*= (include/tensor.cuh:1210-1237). */
+gbla_status gbla_sscal(int64_t len, float alpha, float *x, cudaStream_t stream);
+gbla_status gbla_dscal(int64_t len, double alpha, double *x, cudaStream_t stream);
+
+/* Whole-buffer reductions with a deterministic fixed-order two-pass tree.
+ * The scalar result is written to the device pointer `result`; `workspace`
+ * must hold gbla_reduce_workspace_bytes() bytes.
+ *   dot  : sum x_i y_i          replaces cublas<t>dot   (include/tensor.cuh:968-992)
+ *   nrm2 : sqrt(sum x_i^2)      replaces cublas<t>nrm2  (include/tensor.cuh:994-1010)
+ *   asum : sum |x_i|            replaces cublas<t>asum  (include/tensor.cuh:1012-1028)
+ *   amax : max |x_i|            replaces cublasI<t>amax + element read (include/tensor.cuh:1030-1050)
+ *   amin : min |x_i|            replaces cublasI<t>amin + element read (include/tensor.cuh:1052-1072) */
+size_t gbla_reduce_workspace_bytes(void);
+gbla_status gbla_sdot(int64_t len, const float *x, const float *y, float *result, void *workspace,
+                      cudaStream_t stream);
+gbla_status gbla_ddot(int64_t len, const double *x, const double *y, double *result,
+                      void *workspace, cudaStream_t stream);
+gbla_status gbla_snrm2(int64_t len, const float *x, float *result, void *workspace, cudaStream_t stream);
+gbla_status gbla_dnrm2(int64_t len, const double *x, double *result, void *workspace, cudaStream_t stream);
+gbla_status gbla_sasum(int64_t len, const float *x, float *result, void *workspace, cudaStream_t stream);
+gbla_status gbla_dasum(int64_t len, const double *x, double *result, void *workspace, cudaStream_t stream);
+gbla_status gbla_samax(int64_t len, const float *x, float *result, void *workspace, cudaStream_t stream);
+gbla_status gbla_damax(int64_t len, const double *x, double *result, void *workspace, cudaStream_t stream);
+gbla_status gbla_samin(int64_t len, const float *x, float *result, void *workspace, cudaStream_t stream);
+gbla_status gbla_damin(int64_t len, const double *x, double *result, void *workspace, cudaStream_t stream);
+
+/* Rows [row_from, row_from + nrows) of the m x n matrix A, copied into the
+ * nrows x n matrix out.  Replaces the loop of cublas<t>copy in
+ * DTensor::getRows (include/tensor.cuh:1396-1424). */
+gbla_status gbla_scopy_rows(int m, int n, int row_from, int nrows, const float *A, float *out,
+                            cudaStream_t stream);
+gbla_status gbla_dcopy_rows(int m, int n, int row_from, int nrows, const double *A, double *out,
+                            cudaStream_t stream);
+
+/* -------------------------------------------------------- diagnostics */
+/* Measured FMA throughput of the device (precision 32 or 64), in GFLOP/s,
+ * from a register-resident FMA probe on every SM.  Allocates and
+ * synchronises; for roofline denominators only, never on a hot path. */
+gbla_status gbla_diag_fma_throughput(int precision, int iters, double *gflops, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBLA_H */
