@@ -1,0 +1,573 @@
+#!/usr/bin/env python
+"""Benchmark of the batched-matrix hot path on GB300.
+
+Default workload (one "step"): the precision configuration of the headline
+metric --
+  * DTensor::addAB on 16384 pairs of 64x64 fp32 matrices (entries U[-1,1]),
+    tcgen05 tensor cores with a three-way BF16 split (6 products, FP32
+    accumulation), and
+  * leastSquaresBatched on 8192 tall 128x32 fp32 matrices (U diag(s) V^T,
+    Haar U, V, s log-spaced 1..1e3) with 4 right-hand sides, FP32 Householder
+    QR plus one step of augmented-system refinement with double-FP32
+    residuals.
+value = (16384 + 8192) matrices per step / device time per step, inputs
+resident in HBM (each step has its own copy of the least-squares inputs,
+which the solver overwrites; every step's inputs exceed the 129 MB L2).
+
+Other workloads (--workload d1 ...) time the other configurations.
+
+Arms: --impl ours (default) runs this library; --impl reference times the
+reference's path on the host cores.  GPUtils has no CPU implementation (every
+numeric call is cuBLAS/cuSOLVER), so the reference arm runs the FP64 CPU
+restatement of those library algorithms (oracle/), all host threads, on a
+bounded sample of the same workload.  The reference's own cuBLAS/cuSOLVER
+call sequence on the same GPU is reported inside the ours line as
+"reference_library".
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic.json")
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+# algorithmic work per unit (each input read once, each output written once)
+GEMM_BYTES_PER_PAIR = 3 * 64 * 64 * 4                       # A, B in; C out
+GEMM_FLOPS_PER_PAIR = 2 * 64 ** 3
+LS_M, LS_N, LS_RHS = 128, 32, 4
+LS_BYTES_PER_MATRIX = 4 * (LS_M * LS_N + LS_M * LS_RHS + LS_N * LS_RHS)  # A, B in; x out
+LS_FLOPS_PER_MATRIX = (2 * LS_M * LS_N ** 2 - 2 * LS_N ** 3 // 3
+                       + LS_RHS * (4 * LS_M * LS_N - 2 * LS_N ** 2 + LS_N ** 2))
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["d2", "d1"], default="d2")
+    ap.add_argument("--refine", type=int, default=1, help="least-squares refinement steps")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-library", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
+    return ap.parse_args(argv)
+
+
+# ------------------------------------------------------------- distributed
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def dist_init(world: int, backend: str):
+    import torch.distributed as dist
+
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    return dist
+
+
+def aggregate(elapsed_s: float, units_this_rank: float, world: int, dist=None, device=None):
+    """Whole-job throughput: the units all ranks processed over the slowest
+    rank's time (max over ranks)."""
+    if world > 1:
+        import torch
+
+        t = torch.tensor([elapsed_s, units_this_rank], dtype=torch.float64, device=device)
+        tmax = t[:1].clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        return float(tmax.item()), float(t[1].item())
+    return elapsed_s, units_this_rank
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
+                                 f".clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9 and parts[1].isdigit():
+                rows.append(parts)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        maxmhz = max(int(r[2]) for r in rows)
+        loaded = [int(r[1]) for r in rows if float(r[3] or 0) > 0] or [int(r[1]) for r in rows]
+        busy = [int(r[1]) for r in rows if int(r[1]) > 0.3 * maxmhz] or loaded
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": maxmhz, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3] or 0) for r in rows)}
+
+
+# ------------------------------------------------------------- helpers
+def peaks():
+    if os.path.exists(PEAKS_FILE):
+        d = json.load(open(PEAKS_FILE))
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": FALLBACK_PEAKS["hbm_gbs"], "source": "fallback"}
+
+
+def traffic_for(kernel: str):
+    if os.path.exists(TRAFFIC_FILE):
+        return json.load(open(TRAFFIC_FILE)).get(kernel)
+    return None
+
+
+def to_dev(x, dev):
+    import torch
+
+    x = np.asarray(x)
+    return torch.from_numpy(np.ascontiguousarray(x.transpose(0, 2, 1))).to(dev)
+
+
+def from_dev(t, k, m, n):
+    return t.detach().cpu().numpy().reshape(k, n, m).transpose(0, 2, 1)
+
+
+def rel_err(x, ref):
+    x = np.asarray(x, np.float64); ref = np.asarray(ref, np.float64)
+    num = np.sqrt(((x - ref) ** 2).sum(axis=(1, 2)))
+    den = np.sqrt((ref ** 2).sum(axis=(1, 2)))
+    return float((num / np.where(den == 0, 1, den)).max())
+
+
+# ------------------------------------------------------------ CPU baseline
+def _repeat_timed(fn, seconds: float):
+    """Run fn() until `seconds` have passed (at least once); returns (calls, total seconds)."""
+    calls, t0 = 0, time.perf_counter()
+    while True:
+        fn()
+        calls += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            return calls, el
+
+
+def cpu_baseline_d2(seconds: float):
+    """FP64 oracle (OpenMP over matrices, all host threads) on a fixed sample
+    of the d2 workload, repeated for about `seconds`; matrices/s."""
+    from gputils_gb300 import workloads
+    from oracle import oracle as O
+
+    O.set_threads(os.cpu_count() or 1)
+    ng, nl = 2048, 1024
+    A, B = workloads.d2a_gemm(k=ng, seed=12)
+    LA, LB = workloads.d2b_least_squares(k=nl, seed=13)
+    cg, tg = _repeat_timed(lambda: O.gemm(A, B), seconds * 0.5)
+    cl, tl = _repeat_timed(lambda: O.gels(LA, LB), seconds * 0.5)
+    g_rate, l_rate = cg * ng / tg, cl * nl / tl
+    # one step = 16384 GEMM pairs + 8192 least-squares systems
+    t_step = 16384 / g_rate + 8192 / l_rate
+    return {"value": (16384 + 8192) / t_step, "unit": "matrices/s", "cores": O.max_threads(), "kind": "port",
+            "sample": f"{cg} x {ng} GEMM pairs + {cl} x {nl} least-squares systems in {tg + tl:.1f} s "
+                      f"(FP64, OpenMP over matrices), combined in the 16384 : 8192 ratio of a step",
+            "gemm_pairs_per_s": g_rate, "ls_systems_per_s": l_rate}
+
+
+def cpu_baseline_d1(seconds: float):
+    from gputils_gb300 import workloads
+    from oracle import oracle as O
+
+    O.set_threads(os.cpu_count() or 1)
+    M, b = workloads.d1_cholesky(k=4096, seed=11)
+    calls, t = _repeat_timed(lambda: O.posv(M, b), seconds)
+    return {"value": 4096 * calls / t, "unit": "matrices/s", "cores": O.max_threads(), "kind": "port",
+            "sample": f"{calls} x 4096 16x16 Cholesky factor+solve in {t:.1f} s (FP64, OpenMP over matrices)"}
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if world > 1:
+        dist = dist_init(world, "gloo")
+        if rank != 0:
+            dist.barrier()
+            return
+    # each step is a bounded sample: about cpu_seconds, and the whole run a few minutes at most
+    budget = max(0.5, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
+    fn = cpu_baseline_d2 if args.workload == "d2" else cpu_baseline_d1
+    for _ in range(args.warmup):
+        fn(min(budget, 2.0))
+    vals = [fn(budget) for _ in range(args.steps)]
+    v = statistics.median([x["value"] for x in vals])
+    first = vals[0]
+    line = {
+        "impl": "reference", "metric": metric_name(args.workload), "value": v, "unit": "matrices/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": workload_config(args.workload),
+        "cpu_baseline": {"value": v, "unit": "matrices/s", "cores": first["cores"], "kind": first["kind"],
+                         "sample": first["sample"]},
+        "e2e": {"value": v, "unit": "matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+
+
+def metric_name(workload):
+    return "matrices/s on 1 GB300 (Chol/QR/SVD batched) vs ref cuSOLVER build at equal FP64 err"
+
+
+def workload_config(workload):
+    if workload == "d2":
+        return {"workload": "precision: addAB 16384 x 64x64x64 fp32 (BF16x6 tcgen05) + leastSquaresBatched "
+                            "8192 x 128x32 fp32, 4 RHS, kappa 1e3 (FP32 QR + double-FP32 refinement)",
+                "gemm_pairs": 16384, "ls_systems": 8192, "parallelism": "replicas",
+                "l2": "inputs larger than L2 every step (per-step copies of the least-squares inputs)"}
+    return {"workload": "Cholesky factor+solve 4096 x 16x16 fp32, 1 RHS (CholeskyBatchFactoriser API: potrf + potrs)",
+            "matrices": 4096, "parallelism": "replicas",
+            "l2": "L2 flushed between timed steps (the 4.5 MB working set fits in L2)"}
+
+
+# ------------------------------------------------------------- ours: d2
+class RefLib:
+    def __init__(self, stream):
+        from gputils_gb300 import build
+
+        path = build.BASELINE_LIB
+        if not os.path.exists(path):
+            build.build_baseline()
+        self.L = C.CDLL(path)
+        vp, ip = C.c_void_p, C.c_int
+        self.L.refp_init.argtypes = [vp]
+        self.L.refp_sgemm_batched.argtypes = [ip, ip, ip, C.c_float, vp, vp, C.c_float, vp, ip]
+        self.L.refp_sgels_batched.argtypes = [ip, ip, vp, vp, ip, vp]
+        self.L.refp_spotrf_batched.argtypes = [ip, vp, vp, ip]
+        self.L.refp_spotrs_batched.argtypes = [ip, vp, vp, vp, ip]
+        assert self.L.refp_init(stream) == 0
+
+
+def ptr_array(t, count, stride_elems, dev):
+    import torch
+
+    base = t.data_ptr()
+    return (torch.arange(count, dtype=torch.int64, device=dev) * (stride_elems * t.element_size()) + base)
+
+
+def run_ours_d2(args, dev, st, L, rank, world, dist):
+    import torch
+    from gputils_gb300 import workloads, _lib
+    from oracle import oracle as O
+
+    A, B = workloads.d2a_gemm()
+    LA, LB = workloads.d2b_least_squares()
+    kg, kl = A.shape[0], LA.shape[0]
+    Ag, Bg = to_dev(A, dev), to_dev(B, dev)
+    Cg = torch.empty_like(Ag)
+    LA0, LB0 = to_dev(LA, dev), to_dev(LB, dev)
+    nsteps = args.warmup + args.steps
+    LAs = [LA0.clone() for _ in range(nsteps)]
+    LBs = [LB0.clone() for _ in range(nsteps)]
+    info = torch.empty(kl, dtype=torch.int32, device=dev)
+    m, n, r = LS_M, LS_N, LS_RHS
+
+    def step(i, evs=None):
+        if evs: evs[0].record()
+        _lib.check(L.gbla_sgemm_batched(64, 64, 64, 1.0, Ag.data_ptr(), 4096, Bg.data_ptr(), 4096, 0.0,
+                                        Cg.data_ptr(), 4096, kg, 0, st), "sgemm")
+        if evs: evs[1].record()
+        _lib.check(L.gbla_sgels_batched(m, n, r, LAs[i].data_ptr(), m * n, LBs[i].data_ptr(), m * r,
+                                        info.data_ptr(), args.refine, kl, st), "sgels")
+        if evs: evs[2].record()
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        e0.record()
+        for i in range(args.steps):
+            step(args.warmup + i, evs[i])
+        e1.record()
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    t_gemm = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps / 1e3
+    t_ls = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps / 1e3
+    units = (kg + kl) * args.steps
+    elapsed_max, units_all = aggregate(elapsed, units, world, dist, dev)
+    assert gbla_device_flags_ok(L)
+
+    # accuracy vs the FP64 oracle on a sample
+    idx_g = np.arange(0, kg, 128)
+    err_gemm = rel_err(from_dev(Cg, kg, 64, 64)[idx_g], O.gemm(A[idx_g], B[idx_g]))
+    idx_l = np.arange(0, kl, 64)
+    X = from_dev(LBs[args.warmup], kl, m, r)[idx_l, :n]
+    _, Xo = O.gels(LA[idx_l], LB[idx_l])
+    err_ls = rel_err(X, Xo[:, :n])
+    info_ok = bool((info.cpu().numpy() == 0).all())
+
+    # ---- end to end through the C ABI with host buffers (pinned), copies timed
+    hA, hB = torch.from_numpy(np.ascontiguousarray(A.transpose(0, 2, 1))).pin_memory(), \
+        torch.from_numpy(np.ascontiguousarray(B.transpose(0, 2, 1))).pin_memory()
+    hLA, hLB = torch.from_numpy(np.ascontiguousarray(LA.transpose(0, 2, 1))).pin_memory(), \
+        torch.from_numpy(np.ascontiguousarray(LB.transpose(0, 2, 1))).pin_memory()
+    hC = torch.empty_like(hA).pin_memory()
+    hX = torch.empty_like(hLB).pin_memory()
+    dLA, dLB = torch.empty_like(LA0), torch.empty_like(LB0)
+
+    def e2e_step():
+        Ag.copy_(hA, non_blocking=True); Bg.copy_(hB, non_blocking=True)
+        dLA.copy_(hLA, non_blocking=True); dLB.copy_(hLB, non_blocking=True)
+        _lib.check(L.gbla_sgemm_batched(64, 64, 64, 1.0, Ag.data_ptr(), 4096, Bg.data_ptr(), 4096, 0.0,
+                                        Cg.data_ptr(), 4096, kg, 0, st), "sgemm")
+        _lib.check(L.gbla_sgels_batched(m, n, r, dLA.data_ptr(), m * n, dLB.data_ptr(), m * r, info.data_ptr(),
+                                        args.refine, kl, st), "sgels")
+        hC.copy_(Cg, non_blocking=True); hX.copy_(dLB, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    esteps = max(3, min(args.steps, 10))
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(esteps):
+        e2e_step()
+    f1.record()
+    torch.cuda.synchronize()
+    e2e_t = f0.elapsed_time(f1) / 1e3 / esteps
+    e2e_max, _ = aggregate(e2e_t, 0.0, world, dist, dev)
+    h2d = (hA.numel() + hB.numel() + hLA.numel() + hLB.numel()) * 4
+    d2h = (hC.numel() + hX.numel()) * 4
+
+    # ---- reference library path (cuBLAS / cuSOLVER calls of tensor.cuh) on the same GPU
+    reflib = None
+    if not args.no_reference_library:
+        try:
+            reflib = reference_library_d2(dev, st, Ag, Bg, Cg, LA0, LB0, A, B, LA, LB)
+        except Exception as exc:  # reported, never fatal for our own numbers
+            reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
+
+    pk = peaks()
+    rl = {}
+    for name, t, bytes_, units_k in (("gemm", t_gemm, GEMM_BYTES_PER_PAIR, kg), ("gels", t_ls, LS_BYTES_PER_MATRIX, kl)):
+        ach = bytes_ * units_k / t / 1e9
+        tr = traffic_for(name + "_d2")
+        rl[name] = {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                    "frac": ach / pk["hbm_gbs"], "traffic": tr, "ms": t * 1e3,
+                    "algorithmic_bytes_per_launch": bytes_ * units_k, "peak_source": pk["source"] + " hbm_gbs"}
+    dom = "gemm" if t_gemm >= t_ls else "gels"
+    value = units_all / elapsed_max
+    line = {
+        "metric": metric_name("d2"), "value": value, "unit": "matrices/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_max / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy generators, configuration distributions)",
+        "config": dict(workload_config("d2"), refine_steps=args.refine),
+        "roofline": dict(rl[dom], kernel=dom),
+        "roofline_all": rl,
+        "max_rel_err_vs_fp64": {"gemm": err_gemm, "least_squares_x": err_ls},
+        "info_all_zero": info_ok,
+        "e2e": {"value": (kg + kl) * world / e2e_max, "unit": "matrices/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_max * 1e3,
+                "path": "C ABI (gbla_sgemm_batched + gbla_sgels_batched) with pinned host buffers, "
+                        "H2D of A, B, A_ls, B_ls and D2H of C, X inside the timed region"},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+        "reference_library": reflib,
+    }
+    return line
+
+
+def gbla_device_flags_ok(L):
+    return L.gbla_device_error_flags() == 0
+
+
+def reference_library_d2(dev, st, Ag, Bg, Cg, LA0, LB0, A, B, LA, LB):
+    """The reference's calls on the same inputs: cublasSgemmBatched with
+    pointer arrays (addAB) and cublasSgelsBatched (nrhs = 1, so the 4 RHS run
+    as one call on a 4x-replicated batch; replication not timed)."""
+    import torch
+    from oracle import oracle as O
+
+    R = RefLib(st)
+    kg, kl = Ag.shape[0], LA0.shape[0]
+    m, n, r = LS_M, LS_N, LS_RHS
+    Cr = torch.empty_like(Cg)
+    pa, pb, pc = ptr_array(Ag, kg, 4096, dev), ptr_array(Bg, kg, 4096, dev), ptr_array(Cr, kg, 4096, dev)
+    # replicated least-squares batch: system (i, c) = (A_i, column c of B_i)
+    LAr = LA0.repeat_interleave(r, dim=0).contiguous()                      # (4k, n, m)
+    LBr = LB0.reshape(kl, r, m).reshape(kl * r, 1, m).contiguous()          # (4k, 1, m)
+    LAr0, LBr0 = LAr.clone(), LBr.clone()
+    pla, plb = ptr_array(LAr, kl * r, m * n, dev), ptr_array(LBr, kl * r, m, dev)
+    hinfo = C.c_int(0)
+
+    def gemm():
+        assert R.L.refp_sgemm_batched(64, 64, 64, 1.0, pa.data_ptr(), pb.data_ptr(), 0.0, pc.data_ptr(), kg) == 0
+
+    def gels():
+        assert R.L.refp_sgels_batched(m, n, pla.data_ptr(), plb.data_ptr(), kl * r, C.byref(hinfo)) == 0
+
+    gemm(); LAr.copy_(LAr0); LBr.copy_(LBr0); gels()
+    torch.cuda.synchronize()
+    reps = 5
+    tg = tl = 0.0
+    for _ in range(reps):
+        LAr.copy_(LAr0); LBr.copy_(LBr0)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record(); gemm(); e[1].record(); gels(); e[2].record()
+        torch.cuda.synchronize()
+        tg += e[0].elapsed_time(e[1]) / 1e3
+        tl += e[1].elapsed_time(e[2]) / 1e3
+    tg /= reps; tl /= reps
+    idx = np.arange(0, kg, 128)
+    err_g = rel_err(from_dev(Cr, kg, 64, 64)[idx], O.gemm(A[idx], B[idx]))
+    X = LBr.reshape(kl, r, m).cpu().numpy().transpose(0, 2, 1)[:, :n]
+    idl = np.arange(0, kl, 64)
+    _, Xo = O.gels(LA[idl], LB[idl])
+    err_l = rel_err(X[idl], Xo[:, :n])
+    return {"value": (kg + kl) / (tg + tl), "unit": "matrices/s", "gemm_ms": tg * 1e3, "gels_ms": tl * 1e3,
+            "max_rel_err_vs_fp64": {"gemm": err_g, "least_squares_x": err_l},
+            "calls": "cublasSgemmBatched (pointer arrays) + cublasSgelsBatched on the 4x-replicated batch "
+                     "(one call; nrhs = 1 in the reference API)"}
+
+
+def run_ours_d1(args, dev, st, L, rank, world, dist):
+    """CholeskyBatchFactoriser factorise() + solve() on 4096 16x16: the
+    reference API path (2 launches: potrf, potrs)."""
+    import torch
+    from gputils_gb300 import workloads, _lib
+    from oracle import oracle as O
+
+    M, b = workloads.d1_cholesky()
+    k, n = M.shape[0], M.shape[1]
+    nsteps = args.warmup + args.steps
+    Ms = [to_dev(M, dev) for _ in range(nsteps)]
+    bs = [to_dev(b, dev) for _ in range(nsteps)]
+    info = torch.empty(k, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(i):
+        _lib.check(L.gbla_spotrf_batched(n, Ms[i].data_ptr(), n * n, info.data_ptr(), k, st), "spotrf")
+        _lib.check(L.gbla_spotrs_batched(n, 1, Ms[i].data_ptr(), n * n, bs[i].data_ptr(), n, k, st), "spotrs")
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record(); step(args.warmup + i); e[1].record()
+            torch.cuda.synchronize()
+            times.append(e[0].elapsed_time(e[1]) / 1e3)
+    elapsed = sum(times)
+    elapsed_max, units_all = aggregate(elapsed, k * args.steps, world, dist, dev)
+    x = from_dev(bs[args.warmup], k, n, 1)
+    idx = np.arange(0, k, 16)
+    _, xo, _ = O.posv(M[idx], b[idx])
+    err = rel_err(x[idx], xo)
+    pk = peaks()
+    bytes_ = 4 * (n * n + n * (n + 1) // 2 + 2 * n) * k
+    t = elapsed / args.steps
+    ach = bytes_ / t / 1e9
+    return {
+        "metric": metric_name("d1"), "value": units_all / elapsed_max, "unit": "matrices/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_max / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": workload_config("d1"),
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach / pk["hbm_gbs"], "traffic": traffic_for("chol_d1"), "kernel": "potrf+potrs"},
+        "max_rel_err_vs_fp64": {"x": err}, "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
+        "e2e": None,
+    }
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+    import torch
+    from gputils_gb300 import build, _lib
+
+    rank, world, local = dist_env()
+    dist = dist_init(world, "nccl") if world > 1 else None
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if rank == 0:
+        build.build_lib()
+    if world > 1:
+        dist.barrier()
+    L = _lib.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    if args.workload == "d2":
+        line = run_ours_d2(args, dev, st, L, rank, world, dist)
+        cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline_d2(args.cpu_seconds)
+    else:
+        line = run_ours_d1(args, dev, st, L, rank, world, dist)
+        cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline_d1(args.cpu_seconds)
+    line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -73,5 +73,24 @@ def build_lib(verbose: bool = False, jobs: int | None = None) -> str:
     return LIB
 
 
+BASELINE_SRC = os.path.join(ROOT, "baseline", "ref_path.cu")
+BASELINE_LIB = os.path.join(ROOT, "baseline", "libref_path.so")
+
+
+def build_baseline(verbose: bool = False) -> str:
+    """libref_path.so: the reference's cuBLAS/cuSOLVER call sequence, used
+    only by bench.py to time the reference library path on the same GPU."""
+    if _stale(BASELINE_LIB, [BASELINE_SRC]):
+        cmd = [nvcc(), *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", BASELINE_SRC, "-o",
+               BASELINE_LIB, "-lcublas", "-lcusolver"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"baseline build failed:\n{r.stdout}\n{r.stderr}")
+    return BASELINE_LIB
+
+
 if __name__ == "__main__":
     print(build_lib(verbose=True))
+    print(build_baseline(verbose=True))

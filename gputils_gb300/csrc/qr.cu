@@ -1,0 +1,538 @@
+// qr.cu -- batched Householder QR, Q^T / Q application, upper-triangular
+// solve, and least squares with extended-precision iterative refinement.
+//
+// Layout: one warp per matrix (m <= 128, n <= 32).  Lane l owns rows
+// l + 32 t (t < R = ceil(m/32)) of A in registers; the Householder vector of
+// step k lives in column k below the diagonal (LAPACK dgeqr2/dlarfg
+// convention: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta).  The
+// 32 column dot products of one step are reduced with a butterfly
+// reduce-scatter (31 shuffles for all columns) and broadcast back.
+//
+// Least squares refinement (augmented system of Bjorck): with x and the
+// residual r carried as FP32 pairs (hi + lo), each step computes
+//   f = b - r - A x,   g = -A^T r
+// with error-free products and compensated sums (double-FP32 arithmetic,
+// about 48 significant bits; the device's FP64 rate is ~1/74 of FP32), then
+// solves the correction with the FP32 factors:
+//   h = R^-T g,  d = Q^T f,  dx = R^-1 (d_1 - h),  dr = Q [h; d_2].
+// The original A is kept in shared memory for the residuals.
+#include "common.cuh"
+
+namespace gbla {
+
+enum QrFlags { QR_WRITE_FACTORS = 1, QR_WRITE_TAU = 2, QR_SOLVE = 4 };
+
+// --------------------------------------------------------- double-FP32
+struct ff {
+    float h, l;
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// acc += a * (xh + xl) with an error-free product of a * xh
+__device__ __forceinline__ void ff_fma(ff &acc, float a, float xh, float xl) {
+    float p = a * xh;
+    float pe = fmaf(a, xh, -p);
+    float s, e;
+    two_sum(acc.h, p, s, e);
+    acc.h = s;
+    acc.l += e + pe;
+    acc.l = fmaf(a, xl, acc.l);
+}
+
+__device__ __forceinline__ void ff_add(ff &acc, float xh, float xl) {
+    float s, e;
+    two_sum(acc.h, xh, s, e);
+    acc.h = s;
+    acc.l += e + xl;
+}
+
+__device__ __forceinline__ ff ff_norm(ff a) {
+    float s = a.h + a.l;
+    float e = a.l - (s - a.h);
+    return {s, e};
+}
+
+__device__ __forceinline__ ff ff_warp_sum(ff a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float oh = shfl_xor(a.h, o), ol = shfl_xor(a.l, o);
+        float s, e;
+        two_sum(a.h, oh, s, e);
+        a.h = s;
+        a.l += ol + e;
+    }
+    return ff_norm(a);
+}
+
+// ------------------------------------------------------------ butterfly
+// On entry p[j] is this lane's partial for slot j (32 slots); on exit the
+// return value is the warp-wide total of slot `lane`.
+template <typename T>
+__device__ __forceinline__ T reduce_scatter32(T (&p)[32], int lane) {
+    T q[16];
+    const bool b4 = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        T mine = b4 ? p[i + 16] : p[i];
+        T other = b4 ? p[i] : p[i + 16];
+        q[i] = mine + shfl_xor(other, 16);
+    }
+    const bool b3 = lane & 8;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        T mine = b3 ? q[i + 8] : q[i];
+        T other = b3 ? q[i] : q[i + 8];
+        q[i] = mine + shfl_xor(other, 8);
+    }
+    const bool b2 = lane & 4;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        T mine = b2 ? q[i + 4] : q[i];
+        T other = b2 ? q[i] : q[i + 4];
+        q[i] = mine + shfl_xor(other, 4);
+    }
+    const bool b1 = lane & 2;
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        T mine = b1 ? q[i + 2] : q[i];
+        T other = b1 ? q[i] : q[i + 2];
+        q[i] = mine + shfl_xor(other, 2);
+    }
+    const bool b0 = lane & 1;
+    T mine = b0 ? q[1] : q[0];
+    T other = b0 ? q[0] : q[1];
+    return mine + shfl_xor(other, 1);
+}
+
+// --------------------------------------------------------- warp QR core
+template <typename T, int R>
+struct QrWarp {
+    T a[R][32];  // rows lane + 32 t, columns 0..31
+    int lane;
+
+    __device__ __forceinline__ int row(int t) const { return lane + 32 * t; }
+
+    // Householder QR in registers; tau written to tau_s[k] (shared, per warp).
+    __device__ __forceinline__ int factor(int m, int n, T *tau_s) {
+        int rank_fail = 0;
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            if (k < n) {
+                T x2 = T(0);
+#pragma unroll
+                for (int t = 0; t < R; t++)
+                    if (row(t) > k && row(t) < m) x2 = fma(a[t][k], a[t][k], x2);
+                x2 = warp_sum(x2);
+                const T alpha = shfl(a[0][k], k);
+                T tau = T(0);
+                if (x2 > T(0)) {
+                    const T beta = -copysign(dev_sqrt<T>(fma(alpha, alpha, x2)), alpha);
+                    tau = (beta - alpha) / beta;
+                    const T scal = T(1) / (alpha - beta);
+#pragma unroll
+                    for (int t = 0; t < R; t++)
+                        if (row(t) > k) a[t][k] *= scal;
+                    if (lane == k) a[0][k] = beta;
+                    // w_j = v^T a_j for all slots, then a_j -= tau w_j v
+                    T p[32];
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        T s = T(0);
+                        if (j > k) {
+#pragma unroll
+                            for (int t = 0; t < R; t++) {
+                                T v = row(t) > k ? a[t][k] : (row(t) == k ? T(1) : T(0));
+                                s = fma(v, a[t][j], s);
+                            }
+                        }
+                        p[j] = s;
+                    }
+                    T w = reduce_scatter32(p, lane);
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        if (j > k && j < n) {
+                            T twj = tau * shfl(w, j);
+#pragma unroll
+                            for (int t = 0; t < R; t++) {
+                                T v = row(t) > k ? a[t][k] : (row(t) == k ? T(1) : T(0));
+                                a[t][j] = fma(-twj, v, a[t][j]);
+                            }
+                        }
+                    }
+                }
+                if (lane == 0) tau_s[k] = tau;
+                if (shfl(a[0][k], k) == T(0) && rank_fail == 0) rank_fail = k + 1;
+            }
+        }
+        __syncwarp();
+        return rank_fail;
+    }
+
+    // y <- H_k y for one column held as y[t] (rows lane + 32 t)
+    __device__ __forceinline__ void apply_h(int k, T tau, T (&y)[R]) const {
+        T s = T(0);
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            T v = row(t) > k ? a[t][k] : (row(t) == k ? T(1) : T(0));
+            s = fma(v, y[t], s);
+        }
+        s = tau * warp_sum(s);
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            T v = row(t) > k ? a[t][k] : (row(t) == k ? T(1) : T(0));
+            y[t] = fma(-s, v, y[t]);
+        }
+    }
+
+    __device__ __forceinline__ void apply_qt(int n, const T *tau_s, T (&y)[R]) const {
+#pragma unroll
+        for (int k = 0; k < 32; k++)
+            if (k < n) apply_h(k, tau_s[k], y);
+    }
+
+    __device__ __forceinline__ void apply_q(int n, const T *tau_s, T (&y)[R]) const {
+#pragma unroll
+        for (int k = 31; k >= 0; k--)
+            if (k < n) apply_h(k, tau_s[k], y);
+    }
+
+    // Solve R z = y (y in lane j for j < n); returns z in lane j.
+    __device__ __forceinline__ T back_solve(int n, T y) const {
+        T z = T(0);
+#pragma unroll
+        for (int j = 31; j >= 0; j--) {
+            if (j < n) {
+                T zj = shfl(y / a[0][j], j);  // lane j holds y_j and R_jj
+                if (lane == j) z = zj;
+                if (lane < j) y = fma(-a[0][j], zj, y);
+            }
+        }
+        return z;
+    }
+
+    // Solve R^T h = g (g in lane j); returns h in lane j.
+    __device__ __forceinline__ T forward_solve_rt(int n, T g) const {
+        T h = T(0);
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            if (j < n) {
+                T part = lane < j ? a[0][j] * h : T(0);  // R_ij h_i, i < j
+                T s = warp_sum(part);
+                T hj = (g - s) / a[0][j];
+                if (lane == j) h = hj;
+            }
+        }
+        return h;
+    }
+};
+
+// Augmented-system refinement of one right-hand side (FP32 data, double-FP32
+// residuals).  x0: FP32 solution in lane j; returns the refined x in lane j.
+template <int R>
+__device__ __forceinline__ float refine_ls(const QrWarp<float, R> &q, const float *A0, int m, int n,
+                                           const float (&b)[R], float x0, const float *tau_s, int refine) {
+    constexpr int LDM = 32 * R;
+    const int lane = q.lane;
+    float xh = x0, xl = 0.f;
+    float rh[R], rl[R];
+#pragma unroll
+    for (int t = 0; t < R; t++) { rh[t] = 0.f; rl[t] = 0.f; }
+    for (int it = 0; it <= refine; it++) {
+        // f = b - r - A x  (rows)
+        ff f[R];
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            f[t].h = b[t]; f[t].l = 0.f;
+            ff_add(f[t], -rh[t], -rl[t]);
+        }
+        for (int j = 0; j < n; j++) {
+            float xjh = shfl(xh, j), xjl = shfl(xl, j);
+#pragma unroll
+            for (int t = 0; t < R; t++) {
+                int r = lane + 32 * t;
+                float aij = r < m ? A0[j * LDM + r] : 0.f;
+                ff_fma(f[t], -aij, xjh, xjl);
+            }
+        }
+        if (it == 0) {
+            // first pass: adopt the accurate residual of the FP32 solution as r
+#pragma unroll
+            for (int t = 0; t < R; t++) {
+                ff fn = ff_norm(f[t]);
+                rh[t] = fn.h; rl[t] = fn.l;
+            }
+            continue;
+        }
+        // g = -A^T r (lane j keeps column j)
+        float gj = 0.f;
+        for (int j = 0; j < n; j++) {
+            ff acc = {0.f, 0.f};
+#pragma unroll
+            for (int t = 0; t < R; t++) {
+                int r = lane + 32 * t;
+                float aij = r < m ? A0[j * LDM + r] : 0.f;
+                ff_fma(acc, aij, rh[t], rl[t]);
+            }
+            acc = ff_warp_sum(acc);
+            if (lane == j) gj = -(acc.h + acc.l);
+        }
+        float fr[R];
+#pragma unroll
+        for (int t = 0; t < R; t++) fr[t] = f[t].h + f[t].l;
+        float h = q.forward_solve_rt(n, gj);
+        q.apply_qt(n, tau_s, fr);                       // d = Q^T f
+        float dx = q.back_solve(n, lane < n ? fr[0] - h : 0.f);
+        float z[R];
+#pragma unroll
+        for (int t = 0; t < R; t++) z[t] = (lane + 32 * t) < n ? h : fr[t];
+        q.apply_q(n, tau_s, z);                         // dr = Q [h; d2]
+        {
+            float s, e;
+            two_sum(xh, dx, s, e);
+            float l = xl + e;
+            xh = s + l; xl = l - (xh - s);
+        }
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            float s, e;
+            two_sum(rh[t], z[t], s, e);
+            float l = rl[t] + e;
+            rh[t] = s + l; rl[t] = l - (rh[t] - s);
+        }
+    }
+    return xh + xl;
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(128, 1)
+    k_qr_warp(int m, int n, int nrhs, T *__restrict__ A, int64_t sA, T *__restrict__ B, int64_t sB,
+              T *__restrict__ tau_g, int64_t sTau, int *__restrict__ info, int flags, int refine, int batch) {
+    extern __shared__ __align__(16) unsigned char qsm_raw[];
+    T *qsm = reinterpret_cast<T *>(qsm_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int LDM = 32 * R;
+    constexpr bool kRefinable = sizeof(T) == 4;  // double needs no extended precision
+    if (!kRefinable) refine = 0;
+    // per warp: [original A, LDM x 32, only when refining] [32 taus]
+    const int a0_elems = refine > 0 ? LDM * 32 : 0;
+    T *A0 = qsm + warp * (a0_elems + 32);
+    T *tau_s = A0 + a0_elems;
+    const int64_t mat = (int64_t)blockIdx.x * 4 + warp;
+    if (mat >= batch) return;  // whole warp leaves together; no block barriers below
+    QrWarp<T, R> q;
+    q.lane = lane;
+    T *a_g = A + mat * sA;
+#pragma unroll
+    for (int j = 0; j < 32; j++)
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            int r = lane + 32 * t;
+            T v = (j < n && r < m) ? a_g[(int64_t)j * m + r] : T(0);
+            q.a[t][j] = v;
+            if (refine > 0) A0[j * LDM + r] = v;
+        }
+    int fail = q.factor(m, n, tau_s);
+    if (info && lane == 0) info[mat] = fail;
+
+    if ((flags & QR_SOLVE) && nrhs > 0) {
+        T *b_g = B + mat * sB;
+        for (int c = 0; c < nrhs; c++) {
+            T y[R], b[R];
+#pragma unroll
+            for (int t = 0; t < R; t++) {
+                int r = lane + 32 * t;
+                b[t] = r < m ? b_g[(int64_t)c * m + r] : T(0);
+                y[t] = b[t];
+            }
+            q.apply_qt(n, tau_s, y);
+            T x = q.back_solve(n, lane < n ? y[0] : T(0));
+            if constexpr (kRefinable) {
+                if (refine > 0) x = refine_ls<R>(q, A0, m, n, b, x, tau_s, refine);
+            }
+            // rows < n: solution (row r = this lane when t = 0, since n <= 32);
+            // rows >= n: (Q^T b)(n:m), as gels leaves them
+#pragma unroll
+            for (int t = 0; t < R; t++) {
+                int r = lane + 32 * t;
+                if (r < m) b_g[(int64_t)c * m + r] = r < n ? x : y[t];
+            }
+        }
+    }
+    if (flags & QR_WRITE_FACTORS) {
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+#pragma unroll
+            for (int t = 0; t < R; t++) {
+                int r = lane + 32 * t;
+                if (j < n && r < m) a_g[(int64_t)j * m + r] = q.a[t][j];
+            }
+    }
+    if ((flags & QR_WRITE_TAU) && tau_g && lane < n) tau_g[mat * sTau + lane] = tau_s[lane];
+}
+
+// --------------------------------------------- standalone ormqr / trsm
+// ormqr (left): C <- Q^T C (trans) or Q C, reflectors from a geqrf output.
+template <typename T, int R>
+__global__ void __launch_bounds__(128) k_ormqr_warp(int trans, int m, int nc, int kk, const T *__restrict__ A,
+                                                    int64_t sA, const T *__restrict__ tau, int64_t sTau,
+                                                    T *__restrict__ Cm, int64_t sC, int batch) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t mat = (int64_t)blockIdx.x * 4 + warp;
+    if (mat >= batch) return;
+    const T *a = A + mat * sA;
+    const T *tg = tau + mat * sTau;
+    for (int c = 0; c < nc; c++) {
+        T *col = Cm + mat * sC + (int64_t)c * m;
+        T y[R];
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            int r = lane + 32 * t;
+            y[t] = r < m ? col[r] : T(0);
+        }
+        for (int s = 0; s < kk; s++) {
+            int k = trans ? s : kk - 1 - s;
+            T tk = tg[k];
+            T v[R];
+            T p = T(0);
+#pragma unroll
+            for (int t = 0; t < R; t++) {
+                int r = lane + 32 * t;
+                v[t] = r > k && r < m ? a[(int64_t)k * m + r] : (r == k ? T(1) : T(0));
+                p = fma(v[t], y[t], p);
+            }
+            p = tk * warp_sum(p);
+#pragma unroll
+            for (int t = 0; t < R; t++) y[t] = fma(-p, v[t], y[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            int r = lane + 32 * t;
+            if (r < m) col[r] = y[t];
+        }
+    }
+}
+
+// trsm (left, upper, no transpose, non-unit): B(0:n, :) <- R^-1 B(0:n, :),
+// R = upper triangle of the leading n x n block of a matrix with leading
+// dimension ldr; B has leading dimension ldb.
+template <typename T>
+__global__ void __launch_bounds__(128) k_trsm_upper_warp(int n, int nc, const T *__restrict__ Rm, int64_t ldr,
+                                                         int64_t sR, T *__restrict__ Bm, int64_t ldb, int64_t sB,
+                                                         int batch) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t mat = (int64_t)blockIdx.x * 4 + warp;
+    if (mat >= batch) return;
+    const T *r = Rm + mat * sR;
+    for (int c = 0; c < nc; c++) {
+        T *col = Bm + mat * sB + (int64_t)c * ldb;
+        for (int j = n - 1; j >= 0; j--) {
+            __syncwarp();
+            T xj = col[j] / r[(int64_t)j * ldr + j];
+            __syncwarp();
+            for (int i = lane; i < j; i += 32) col[i] = fma(-r[(int64_t)j * ldr + i], xj, col[i]);
+            if (lane == 0) col[j] = xj;
+        }
+        __syncwarp();
+    }
+}
+
+template <typename T>
+static gbla_status qr_launch(int m, int n, int nrhs, T *A, int64_t sA, T *B, int64_t sB, T *tau, int64_t sTau,
+                             int *info, int flags, int refine, int batch, cudaStream_t st) {
+    if (m < 0 || n < 0 || nrhs < 0 || batch < 0 || refine < 0 || m < n) return GBLA_INVALID_VALUE;
+    if (batch == 0 || n == 0) return GBLA_SUCCESS;
+    if (!A || sA < (int64_t)m * n) return GBLA_INVALID_VALUE;
+    if ((flags & QR_SOLVE) && nrhs > 0 && (!B || sB < (int64_t)m * nrhs)) return GBLA_INVALID_VALUE;
+    if ((flags & QR_WRITE_TAU) && (!tau || sTau < n)) return GBLA_INVALID_VALUE;
+    if (m > 128 || n > 32) return GBLA_NOT_SUPPORTED;
+    if (sizeof(T) != 4) refine = 0;
+    const int R = (m + 31) / 32;
+    // shared memory: per warp the original A (refinement only) and 32 taus
+    size_t smem = (size_t)4 * ((refine > 0 ? 32 * R * 32 : 0) + 32) * sizeof(T);
+    const unsigned grid = (unsigned)((batch + 3) / 4);
+    auto go = [&](auto kern) -> gbla_status {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return from_cuda(e);
+        }
+        kern<<<grid, 128, smem, st>>>(m, n, nrhs, A, sA, B, sB, tau, sTau, info, flags, refine, batch);
+        return launch_status();
+    };
+    switch (R) {
+        case 1: return go(k_qr_warp<T, 1>);
+        case 2: return go(k_qr_warp<T, 2>);
+        case 3: return go(k_qr_warp<T, 3>);
+        default: return go(k_qr_warp<T, 4>);
+    }
+}
+
+template <typename T>
+static gbla_status ormqr_launch(int trans, int m, int nc, int k, const T *A, int64_t sA, const T *tau, int64_t sTau,
+                                T *Cm, int64_t sC, int batch, cudaStream_t st) {
+    if (m < 0 || nc < 0 || k < 0 || k > m || batch < 0) return GBLA_INVALID_VALUE;
+    if (batch == 0 || nc == 0 || k == 0 || m == 0) return GBLA_SUCCESS;
+    if (!A || !tau || !Cm || sA < (int64_t)m * k || sTau < k || sC < (int64_t)m * nc) return GBLA_INVALID_VALUE;
+    if (m > 128) return GBLA_NOT_SUPPORTED;
+    const unsigned grid = (unsigned)((batch + 3) / 4);
+    switch ((m + 31) / 32) {
+        case 1: k_ormqr_warp<T, 1><<<grid, 128, 0, st>>>(trans, m, nc, k, A, sA, tau, sTau, Cm, sC, batch); break;
+        case 2: k_ormqr_warp<T, 2><<<grid, 128, 0, st>>>(trans, m, nc, k, A, sA, tau, sTau, Cm, sC, batch); break;
+        case 3: k_ormqr_warp<T, 3><<<grid, 128, 0, st>>>(trans, m, nc, k, A, sA, tau, sTau, Cm, sC, batch); break;
+        default: k_ormqr_warp<T, 4><<<grid, 128, 0, st>>>(trans, m, nc, k, A, sA, tau, sTau, Cm, sC, batch); break;
+    }
+    return launch_status();
+}
+
+template <typename T>
+static gbla_status trsm_launch(int n, int nc, const T *Rm, int64_t ldr, int64_t sR, T *Bm, int64_t ldb, int64_t sB,
+                               int batch, cudaStream_t st) {
+    if (n < 0 || nc < 0 || batch < 0 || ldr < n || ldb < n) return GBLA_INVALID_VALUE;
+    if (batch == 0 || n == 0 || nc == 0) return GBLA_SUCCESS;
+    if (!Rm || !Bm || sR < ldr * n || sB < ldb * nc) return GBLA_INVALID_VALUE;
+    k_trsm_upper_warp<T><<<(unsigned)((batch + 3) / 4), 128, 0, st>>>(n, nc, Rm, ldr, sR, Bm, ldb, sB, batch);
+    return launch_status();
+}
+
+}  // namespace gbla
+
+using namespace gbla;
+
+GBLA_API gbla_status gbla_sgeqrf_batched(int m, int n, float *A, int64_t sA, float *tau, int64_t sTau, int *info,
+                                         int batch, cudaStream_t st) {
+    return qr_launch<float>(m, n, 0, A, sA, nullptr, 0, tau, sTau, info, QR_WRITE_FACTORS | QR_WRITE_TAU, 0, batch, st);
+}
+GBLA_API gbla_status gbla_dgeqrf_batched(int m, int n, double *A, int64_t sA, double *tau, int64_t sTau, int *info,
+                                         int batch, cudaStream_t st) {
+    return qr_launch<double>(m, n, 0, A, sA, nullptr, 0, tau, sTau, info, QR_WRITE_FACTORS | QR_WRITE_TAU, 0, batch,
+                             st);
+}
+GBLA_API gbla_status gbla_sgels_batched(int m, int n, int nrhs, float *A, int64_t sA, float *B, int64_t sB, int *info,
+                                        int refine, int batch, cudaStream_t st) {
+    return qr_launch<float>(m, n, nrhs, A, sA, B, sB, nullptr, 0, info, QR_WRITE_FACTORS | QR_SOLVE, refine, batch, st);
+}
+GBLA_API gbla_status gbla_dgels_batched(int m, int n, int nrhs, double *A, int64_t sA, double *B, int64_t sB,
+                                        int *info, int batch, cudaStream_t st) {
+    return qr_launch<double>(m, n, nrhs, A, sA, B, sB, nullptr, 0, info, QR_WRITE_FACTORS | QR_SOLVE, 0, batch, st);
+}
+GBLA_API gbla_status gbla_sormqr_batched(int trans, int m, int nc, int k, const float *A, int64_t sA, const float *tau,
+                                         int64_t sTau, float *Cm, int64_t sC, int batch, cudaStream_t st) {
+    return ormqr_launch<float>(trans, m, nc, k, A, sA, tau, sTau, Cm, sC, batch, st);
+}
+GBLA_API gbla_status gbla_dormqr_batched(int trans, int m, int nc, int k, const double *A, int64_t sA,
+                                         const double *tau, int64_t sTau, double *Cm, int64_t sC, int batch,
+                                         cudaStream_t st) {
+    return ormqr_launch<double>(trans, m, nc, k, A, sA, tau, sTau, Cm, sC, batch, st);
+}
+GBLA_API gbla_status gbla_strsm_upper_batched(int n, int nc, const float *Rm, int64_t ldr, int64_t sR, float *Bm,
+                                              int64_t ldb, int64_t sB, int batch, cudaStream_t st) {
+    return trsm_launch<float>(n, nc, Rm, ldr, sR, Bm, ldb, sB, batch, st);
+}
+GBLA_API gbla_status gbla_dtrsm_upper_batched(int n, int nc, const double *Rm, int64_t ldr, int64_t sR, double *Bm,
+                                              int64_t ldb, int64_t sB, int batch, cudaStream_t st) {
+    return trsm_launch<double>(n, nc, Rm, ldr, sR, Bm, ldb, sB, batch, st);
+}

@@ -103,6 +103,48 @@ gbla_status gbla_dposv_batched(int n, int nrhs, double *A, int64_t strideA, doub
                                int64_t strideB, int *info, int refine_iters, int batch,
                                cudaStream_t stream);
 
+/* -------------------------------------------------------------------- QR */
+/* Householder QR of m x n matrices (m >= n, m <= 128, n <= 32): R in the
+ * upper triangle, the Householder vectors below it (LAPACK dgeqrf
+ * convention), tau (n per matrix, batch stride strideTau).  info[i] = j if
+ * R(j-1, j-1) is exactly zero, else 0 (nullable).
+ * Replaces cusolverDn<t>geqrf (include/tensor.cuh:1866-1889). */
+gbla_status gbla_sgeqrf_batched(int m, int n, float *A, int64_t strideA, float *tau, int64_t strideTau,
+                                int *info, int batch, cudaStream_t stream);
+gbla_status gbla_dgeqrf_batched(int m, int n, double *A, int64_t strideA, double *tau, int64_t strideTau,
+                                int *info, int batch, cudaStream_t stream);
+
+/* C_i <- Q_i^T C_i (trans != 0) or Q_i C_i, Q_i = H_0 ... H_{k-1} from a
+ * geqrf result (A_i m x k, tau_i), C_i m x nc.  m <= 128.
+ * Replaces cusolverDn<t>ormqr (include/tensor.cuh:1891-1927, 1946-1952). */
+gbla_status gbla_sormqr_batched(int trans, int m, int nc, int k, const float *A, int64_t strideA,
+                                const float *tau, int64_t strideTau, float *C, int64_t strideC, int batch,
+                                cudaStream_t stream);
+gbla_status gbla_dormqr_batched(int trans, int m, int nc, int k, const double *A, int64_t strideA,
+                                const double *tau, int64_t strideTau, double *C, int64_t strideC, int batch,
+                                cudaStream_t stream);
+
+/* B_i(0:n, :) <- R_i^-1 B_i(0:n, :) with R_i the upper triangle of the leading
+ * n x n block of a matrix stored with leading dimension ldr; B_i has nc
+ * columns and leading dimension ldb.
+ * Replaces cublas<t>trsm (left, upper, no-trans, non-unit; include/tensor.cuh:1903-1907). */
+gbla_status gbla_strsm_upper_batched(int n, int nc, const float *R, int64_t ldr, int64_t strideR, float *B,
+                                     int64_t ldb, int64_t strideB, int batch, cudaStream_t stream);
+gbla_status gbla_dtrsm_upper_batched(int n, int nc, const double *R, int64_t ldr, int64_t strideR, double *B,
+                                     int64_t ldb, int64_t strideB, int batch, cudaStream_t stream);
+
+/* Least squares min ||A_i x - b_i|| for each of nrhs columns (m >= n,
+ * m <= 128, n <= 32): A_i is overwritten with its QR factors and rows [0, n)
+ * of each B_i column with the solution (rows [n, m) hold (Q^T b)(n:m)).
+ * Single precision: refine_iters steps of augmented-system refinement with
+ * double-FP32 residuals recover FP64-level accuracy of x.  info as geqrf.
+ * Replaces cublas<t>gelsBatched in DTensor::leastSquaresBatched
+ * (include/tensor.cuh:1340-1394), which allows nrhs = 1 only. */
+gbla_status gbla_sgels_batched(int m, int n, int nrhs, float *A, int64_t strideA, float *B, int64_t strideB,
+                               int *info, int refine_iters, int batch, cudaStream_t stream);
+gbla_status gbla_dgels_batched(int m, int n, int nrhs, double *A, int64_t strideA, double *B, int64_t strideB,
+                               int *info, int batch, cudaStream_t stream);
+
 /* ------------------------------------------------------- level-1 / copy */
 /* Per-matrix transpose: At_i (n x m) = A_i^T (A_i is m x n).
  * Replaces the host loop of cublas<t>geam in DTensor::tr (include/tensor.cuh:1167-1197). */
