@@ -1,6 +1,7 @@
 // blas1.cu -- HBM-bound helpers of the DTensor API: batched transpose, axpy,
 // scal, row extraction and deterministic whole-buffer reductions.
 #include <cfloat>
+#include <mutex>
 #include "common.cuh"
 
 namespace gbla {
@@ -175,6 +176,47 @@ static gbla_status reduce(int64_t len, const T *x, const T *y, T *result, void *
     return launch_status();
 }
 
+// Pass-1 block count (= partial sums) of reduce() for len elements; used by
+// gbla_sdot_noalloc so that it launches exactly what gbla_sdot launches.
+static int red_blocks(int64_t len) {
+    int64_t nb = (len + RED_THREADS * 4 - 1) / (RED_THREADS * 4);
+    if (nb < 1) nb = 1;
+    if (nb > RED_MAX_BLOCKS) nb = RED_MAX_BLOCKS;
+    return (int)nb;
+}
+
+// ------------------------------------------------ allocation-free dot product
+// gbla_sdot_noalloc keeps the pass-1 partial sums of the float dot product in
+// this fixed device array instead of a caller workspace.  It holds the most
+// partial sums any length needs (RED_MAX_BLOCKS floats, 4 KB) and stays
+// resident on every device that loads the library until the process exits.
+// Host code may not use the symbol itself as a device address: its address is
+// fetched once per device with cudaGetSymbolAddress (dot_scratch_address).
+constexpr int NOALLOC_DOT_PARTIALS = RED_MAX_BLOCKS;
+static __device__ __align__(256) float g_dot_scratch[NOALLOC_DOT_PARTIALS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_dot_scratch_mu;
+static float *g_dot_scratch_addr[NOALLOC_MAX_DEVICES] = {nullptr};
+
+// Device address of g_dot_scratch on the current device; looked up on the
+// first call for each device (with that device current) and cached.
+static gbla_status dot_scratch_address(float **out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return from_cuda(e);
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return GBLA_NOT_SUPPORTED;
+    std::lock_guard<std::mutex> lock(g_dot_scratch_mu);
+    if (!g_dot_scratch_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_dot_scratch);
+        if (e != cudaSuccess) return from_cuda(e);
+        g_dot_scratch_addr[dev] = static_cast<float *>(p);
+    }
+    *out = g_dot_scratch_addr[dev];
+    return GBLA_SUCCESS;
+}
+
 }  // namespace gbla
 
 using namespace gbla;
@@ -229,4 +271,23 @@ GBLA_API gbla_status gbla_sdot(int64_t len, const float *x, const float *y, floa
 GBLA_API gbla_status gbla_ddot(int64_t len, const double *x, const double *y, double *result, void *ws,
                                cudaStream_t st) {
     return reduce<double, RED_DOT>(len, x, y, result, ws, st);
+}
+
+// Same kernels and block count as gbla_sdot (so the same result bits); the
+// partial sums go to g_dot_scratch.  Pass 1 writes every partial that pass 2
+// reads, so nothing in the array has to start at zero.  Calls that overlap on
+// the GPU share the array and race.
+GBLA_API gbla_status gbla_sdot_noalloc(int64_t len, const float *x, const float *y, float *result, cudaStream_t st) {
+    if (len < 0 || !result) return GBLA_INVALID_VALUE;
+    if (len > 0 && (!x || !y)) return GBLA_INVALID_VALUE;
+    const int nb = red_blocks(len);
+    if (nb > NOALLOC_DOT_PARTIALS) return GBLA_WORKSPACE_TOO_SMALL;  // more partials than the array holds
+    float *parts = nullptr;
+    gbla_status s = dot_scratch_address(&parts);
+    if (s != GBLA_SUCCESS) return s;
+    k_reduce_pass1<float, RED_DOT><<<nb, RED_THREADS, 0, st>>>(len, x, y, parts);
+    s = launch_status();
+    if (s != GBLA_SUCCESS) return s;
+    k_reduce_pass2<float, RED_DOT><<<1, RED_THREADS, 0, st>>>(nb, parts, result);
+    return launch_status();
 }

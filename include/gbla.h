@@ -184,6 +184,24 @@ gbla_status gbla_damax(int64_t len, const double *x, double *result, void *works
 gbla_status gbla_samin(int64_t len, const float *x, float *result, void *workspace, cudaStream_t stream);
 gbla_status gbla_damin(int64_t len, const double *x, double *result, void *workspace, cudaStream_t stream);
 
+/* Allocation-free variant of gbla_sdot, for callers that cannot allocate
+ * device memory: a real-time control loop that must not call cudaMalloc
+ * after start-up, code running while a stream is being captured, or a host
+ * application that owns all device allocation.  It needs no workspace: the
+ * partial sums live in a fixed 4 KB device array inside libgbla.so (1024
+ * floats, the most any length needs; every device that loads the library
+ * keeps it until the process exits).  Same kernels, block count and result
+ * as gbla_sdot.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU (other streams, other host threads) race; serialise them.
+ * Returns GBLA_WORKSPACE_TOO_SMALL if a length would need more than 1024
+ * partial sums (none does with the current block count).  No counterpart in
+ * the reference: GPUtils' dotF (include/tensor.cuh:968-992) goes through
+ * cuBLAS, which manages its own workspace. */
+gbla_status gbla_sdot_noalloc(int64_t len, const float *x, const float *y, float *result,
+                              cudaStream_t stream);
+
 /* Rows [row_from, row_from + nrows) of the m x n matrix A, copied into the
  * nrows x n matrix out.  Replaces the loop of cublas<t>copy in
  * DTensor::getRows (include/tensor.cuh:1396-1424). */
