@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "libgbla.so")
 
 _CTYPES = {
     "int": C.c_int,
+    "unsigned int": C.c_uint,
     "int64_t": C.c_int64,
     "size_t": C.c_size_t,
     "float": C.c_float,
@@ -32,7 +33,7 @@ _DECL = re.compile(r"^\s*([A-Za-z_][\w\s\*]*?)\s*\b(gbla_\w+)\s*\(([^;]*?)\)\s*;
 
 
 def _ctype(tok: str):
-    tok = tok.replace("const", " ").strip()
+    tok = " ".join(tok.replace("const", " ").split())
     if "*" in tok:
         base = tok.replace("*", "").strip()
         return C.c_char_p if base == "char" else C.c_void_p

@@ -145,6 +145,41 @@ gbla_status gbla_sgels_batched(int m, int n, int nrhs, float *A, int64_t strideA
 gbla_status gbla_dgels_batched(int m, int n, int nrhs, double *A, int64_t strideA, double *B, int64_t strideB,
                                int *info, int batch, cudaStream_t stream);
 
+/* ------------------------------------------------------------------- SVD */
+/* One-sided (Hestenes) Jacobi SVD A_i = U_i diag(S_i) Vt_i of m x n matrices
+ * (m >= n; n <= 32 with m <= 64, or n <= 64 with m <= 128), all in FP32.
+ * S_i: n singular values, descending.  Vt_i: n x n (= V^T, as Svd::
+ * rightSingularVectors returns).  U_i: m x m, nullable (computeU = false).
+ * A_i is destroyed (it ends as A_i V_i).  V0 (nullable): n x n orthogonal warm
+ * start; A_i V0_i is orthogonalised and V starts at V0.  A pair of columns is
+ * rotated while |a_p.a_q| > tol |a_p||a_q|; info[i] = 1 if max_sweeps sweeps
+ * did not converge (nullable), sweeps[i] = sweeps used (nullable).  Sign
+ * rule: the largest-magnitude entry of each v_j is negative.
+ * Replaces the host loop of cusolverDn<t>gesvd in Svd<T>::factorise
+ * (include/tensor.cuh:1624-1676). */
+gbla_status gbla_sgesvj_batched(int m, int n, float *A, int64_t strideA, float *S, int64_t strideS, float *Vt,
+                                int64_t strideVt, float *U, int64_t strideU, const float *V0, int64_t strideV0,
+                                float tol, int max_sweeps, int *info, int *sweeps, int batch,
+                                cudaStream_t stream);
+
+/* rank[i] = number of entries of S_i (length len) greater than eps.  Unlike
+ * Svd::rank (include/tensor.cuh:1600-1609, kernel :1484-1491) the count is
+ * written, not accumulated, so repeated calls agree. */
+gbla_status gbla_srank_batched(int len, const float *S, int64_t strideS, float eps, unsigned int *rank, int batch,
+                               cudaStream_t stream);
+
+/* Null space of square or fat m x n matrices (1 <= m <= n <= 64): N_i (n x n)
+ * holds an orthonormal basis of ker(A_i) in its first nullity_i columns
+ * (zero-padded), P_i = N_i N_i^T (n x n).  Singular values <= eps, or
+ * below the FP32 noise level n * FLT_EPSILON * sigma_max, count as zero.  nullity (nullable) receives n - rank.  info as gesvj (nullable).
+ * `workspace` must hold gbla_snullspace_workspace_bytes(m, n, batch) bytes.
+ * Replaces the Nullspace constructor (include/tensor.cuh:2044-2079: tr, Svd of
+ * A^T with U, rank, and per-matrix copies and gemms). */
+size_t gbla_snullspace_workspace_bytes(int m, int n, int batch);
+gbla_status gbla_snullspace_batched(int m, int n, const float *A, int64_t strideA, float *N, float *P,
+                                    unsigned int *nullity, float eps, int *info, void *workspace,
+                                    size_t workspace_bytes, int batch, cudaStream_t stream);
+
 /* ------------------------------------------------------- level-1 / copy */
 /* Per-matrix transpose: At_i (n x m) = A_i^T (A_i is m x n).
  * Replaces the host loop of cublas<t>geam in DTensor::tr (include/tensor.cuh:1167-1197). */
