@@ -14,58 +14,13 @@
 // Refinement (posv) recomputes r = b - A x from the lower triangle of the
 // original A, which stays untouched in global memory until L is stored.
 #include "common.cuh"
+#include "chol_common.cuh"
 
 namespace gbla {
 
-enum CholMode { CH_FACTOR = 1, CH_SOLVE = 2 };
 
 // residual accumulation type of the refinement
 template <typename T> struct ResT { using type = double; };
-
-// ------------------------------------------------------------ lane-row kernel
-template <typename T, int NB>
-__device__ __forceinline__ void lr_factor(T (&a)[NB], T &dinv, int &fail, int n, int r) {
-#pragma unroll
-    for (int k = 0; k < NB; k++) {
-        if (k < n) {
-            T d = shfl(a[k], k, NB);
-            if (!(d > T(0)) && fail == 0) fail = k + 1;
-            T l = dev_sqrt<T>(d);
-            T il = T(1) / l;
-            if (r == k) { a[k] = l; dinv = il; }
-            else if (r > k) a[k] *= il;
-#pragma unroll
-            for (int j = k + 1; j < NB; j++) {
-                if (j < n) {
-                    T ljk = shfl(a[k], j, NB);
-                    if (r >= j) a[j] -= a[k] * ljk;
-                }
-            }
-        }
-    }
-}
-
-// Solve L L^T x = b for one right-hand side held one row per lane.
-template <typename T, int NB>
-__device__ __forceinline__ T lr_solve(const T (&a)[NB], T dinv, T b, int n, int r) {
-#pragma unroll
-    for (int k = 0; k < NB; k++) {
-        if (k < n) {
-            if (r == k) b *= dinv;
-            T yk = shfl(b, k, NB);
-            if (r > k) b -= a[k] * yk;
-        }
-    }
-#pragma unroll
-    for (int k = NB - 1; k >= 0; k--) {
-        if (k < n) {
-            T part = (r > k && r < n) ? a[k] * b : T(0);
-            T s = group_sum(part, NB);
-            if (r == k) b = (b - s) * dinv;
-        }
-    }
-    return b;
-}
 
 // y_r = (A x)_r for symmetric A given by its lower triangle in global memory.
 template <typename T, int NB, typename R>
@@ -138,38 +93,6 @@ __global__ void __launch_bounds__(128, 1) k_chol_lanerow(int n, int nrhs, T *__r
 }
 
 // ------------------------------------------------------------------ CTA kernel
-constexpr int CTA_THREADS = 256;
-constexpr int CTA_WARPS = CTA_THREADS / 32;
-constexpr int CTA_RHS_CHUNK = CTA_WARPS;  // one warp per right-hand side
-
-__host__ __device__ inline int cta_ld(int n) { return n | 1; }
-
-template <typename T>
-__host__ __device__ inline size_t cta_smem_bytes(int n) {
-    int ld = cta_ld(n);
-    return sizeof(T) * ((size_t)n * ld + (size_t)n * CTA_RHS_CHUNK + n) + 16;
-}
-
-// Solve L L^T x = b for the column x (length n, shared memory) with one warp.
-template <typename T>
-__device__ __forceinline__ void cta_solve_col(const T *__restrict__ a, int ld, const T *__restrict__ dinv,
-                                              T *__restrict__ x, int n, int lane) {
-    for (int k = 0; k < n; k++) {
-        T xk = x[k] * dinv[k];
-        for (int i = k + 1 + lane; i < n; i += 32) x[i] -= a[(int64_t)k * ld + i] * xk;
-        __syncwarp();
-        if (lane == 0) x[k] = xk;
-        __syncwarp();
-    }
-    for (int k = n - 1; k >= 0; k--) {
-        T xk = x[k] * dinv[k];
-        for (int i = lane; i < k; i += 32) x[i] -= a[(int64_t)i * ld + k] * xk;  // L(k, i)
-        __syncwarp();
-        if (lane == 0) x[k] = xk;
-        __syncwarp();
-    }
-}
-
 template <typename T>
 __global__ void __launch_bounds__(CTA_THREADS, 1) k_chol_cta(int n, int nrhs, T *__restrict__ A, int64_t sA,
                                                           T *__restrict__ B, int64_t sB, int *__restrict__ info,

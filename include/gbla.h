@@ -103,6 +103,31 @@ gbla_status gbla_dposv_batched(int n, int nrhs, double *A, int64_t strideA, doub
                                int64_t strideB, int *info, int refine_iters, int batch,
                                cudaStream_t stream);
 
+/* Ragged batches: SPD systems of mixed size in one call.  System i has its
+ * n_i x n_i matrix at A + a_offsets[i] and its n_i x nrhs_i right-hand sides
+ * at B + b_offsets[i] (element offsets, column-major, 1 <= n_i <= 128).
+ * The plan sorts the systems into size classes (largest first) once; it owns
+ * a small device table, an auxiliary stream and two events, so create it at
+ * set-up time (it allocates and synchronises) and do not use one plan from
+ * two host threads at once.  No reference counterpart: GPUtils needs one
+ * CholeskyBatchFactoriser per size and one potrs per column
+ * (include/tensor.cuh:2100-2197). */
+typedef struct gbla_ragged_plan gbla_ragged_plan;
+gbla_status gbla_ragged_plan_create(const int64_t *a_offsets, const int64_t *b_offsets, const int *n,
+                                    const int *nrhs, int count, gbla_ragged_plan **plan);
+gbla_status gbla_ragged_plan_destroy(gbla_ragged_plan *plan);
+
+/* Factor + solve every system of the plan (device on which the plan was
+ * created; stream-ordered; graph-capturable).  A_i receives its FP32 Cholesky
+ * factor (lower triangle), B_i the solutions, info[i] the potrf status.  The
+ * factorisation runs in FP32; refine_iters refinement steps recompute
+ * B - A X from the full symmetric original A_i (both triangles must be
+ * stored) in double-FP32 (float) or FP64 (double) and add the FP32 correction. */
+gbla_status gbla_sposv_ragged(const gbla_ragged_plan *plan, float *A, float *B, int *info, int refine_iters,
+                              cudaStream_t stream);
+gbla_status gbla_dposv_ragged(const gbla_ragged_plan *plan, double *A, double *B, int *info, int refine_iters,
+                              cudaStream_t stream);
+
 /* -------------------------------------------------------------------- QR */
 /* Householder QR of m x n matrices (m >= n, m <= 128, n <= 32): R in the
  * upper triangle, the Householder vectors below it (LAPACK dgeqrf

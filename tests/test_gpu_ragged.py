@@ -1,0 +1,125 @@
+"""Ragged batched Cholesky factor + solve + refinement (gbla_{s,d}posv_ragged)
+through the C ABI against the FP64 oracle's per-system potrf + potrs."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gputils_gb300 import workloads
+from oracle import oracle as O
+from tests.helpers import stream
+
+pytestmark = pytest.mark.gpu
+
+
+def _plan(lib, a_off, b_off, n, nrhs):
+    p = C.c_void_p()
+    a_off = np.ascontiguousarray(a_off, np.int64); b_off = np.ascontiguousarray(b_off, np.int64)
+    n = np.ascontiguousarray(n, np.int32); nrhs = np.ascontiguousarray(nrhs, np.int32)
+    st = lib.gbla_ragged_plan_create(a_off.ctypes.data, b_off.ctypes.data, n.ctypes.data, nrhs.ctypes.data,
+                                     len(n), C.byref(p))
+    return st, p
+
+
+def _solve(lib, n, nrhs, a_off, b_off, A, B, dt, refine):
+    import torch
+    st, plan = _plan(lib, a_off, b_off, n, nrhs)
+    assert st == 0
+    Ad = torch.tensor(A.astype(dt)).cuda()
+    Bd = torch.tensor(B.astype(dt)).cuda()
+    info = torch.full((len(n),), -1, dtype=torch.int32, device="cuda")
+    fn = lib.gbla_sposv_ragged if dt == np.float32 else lib.gbla_dposv_ragged
+    assert fn(plan, Ad.data_ptr(), Bd.data_ptr(), info.data_ptr(), refine, stream()) == 0
+    torch.cuda.synchronize()
+    assert lib.gbla_ragged_plan_destroy(plan) == 0
+    return Ad.cpu().numpy(), Bd.cpu().numpy(), info.cpu().numpy()
+
+
+def _max_rel_err(n, nrhs, b_off, X, Xref):
+    worst = 0.0
+    for i in range(len(n)):
+        sl = slice(b_off[i], b_off[i] + n[i] * nrhs[i])
+        if nrhs[i] == 0:
+            continue
+        d = np.linalg.norm(X[sl].astype(np.float64) - Xref[sl]) / np.linalg.norm(Xref[sl])
+        worst = max(worst, d)
+    return worst
+
+
+@pytest.mark.parametrize("dt,refine,tol", [(np.float32, 0, 5e-5), (np.float32, 1, 1e-6), (np.float32, 2, 1e-6),
+                                           (np.float64, 0, 5e-5), (np.float64, 2, 1e-11), (np.float64, 3, 1e-13)])
+def test_mixed_sizes_vs_oracle(gbla_lib, cuda, dt, refine, tol):
+    n, nrhs, a_off, b_off, A, B = workloads.d3_ragged(count=700, seed=21, dtype=np.float64)
+    Af, Xf, info = _solve(gbla_lib, n, nrhs, a_off, b_off, A, B, dt, refine)
+    Ao, Xo, info_o = O.posv_ragged(A.astype(dt), B.astype(dt), a_off, b_off, n, nrhs)
+    assert (info == 0).all() and (info_o == 0).all()
+    err = _max_rel_err(n, nrhs, b_off, Xf, Xo)
+    assert err < tol, err
+    # L in place (FP32 factor), strict upper triangle untouched
+    for i in range(0, len(n), 37):
+        k = n[i]
+        L = Af[a_off[i]:a_off[i] + k * k].reshape(k, k).T
+        Lo = Ao[a_off[i]:a_off[i] + k * k].reshape(k, k).T
+        assert np.abs(np.tril(L) - np.tril(Lo)).max() < 5e-5 * np.abs(Lo).max()
+        Ain = A[a_off[i]:a_off[i] + k * k].reshape(k, k).T.astype(dt)
+        assert np.array_equal(np.triu(L, 1), np.triu(Ain, 1))
+
+
+def test_edges_and_info(gbla_lib, cuda):
+    rng = np.random.default_rng(5)
+    ns = [1, 8, 9, 16, 17, 32, 33, 64, 128, 5, 40]
+    rhs = [1, 0, 8, 3, 1, 2, 5, 1, 8, 2, 3]
+    mats, a_off, b_off, Bs = [], [], [], []
+    ao = bo = 0
+    for k, (nn, r) in enumerate(zip(ns, rhs)):
+        G = rng.standard_normal((nn, nn))
+        M = G.T @ G / nn + 0.1 * np.eye(nn)
+        if k == 9:
+            M[3, 3] = -5.0      # leading minor 4 fails
+        if k == 10:
+            M[39, 39] = -1.0    # last minor fails (large path)
+        mats.append(M.T.ravel()); a_off.append(ao); ao += nn * nn
+        Bs.append(rng.standard_normal(nn * r)); b_off.append(bo); bo += nn * r
+    A, B = np.concatenate(mats), np.concatenate(Bs)
+    _, X, info = _solve(gbla_lib, np.array(ns), np.array(rhs), np.array(a_off), np.array(b_off), A, B,
+                        np.float32, 1)
+    assert list(info[:9]) == [0] * 9 and info[9] == 4 and info[10] == 40
+    _, Xo, _ = O.posv_ragged(A.astype(np.float32), B.astype(np.float32), a_off, b_off, ns, rhs)
+    assert _max_rel_err(ns[:9], rhs[:9], b_off[:9], X, Xo) < 1e-6
+
+
+def test_invalid_plans(gbla_lib, cuda):
+    st, _ = _plan(gbla_lib, [0], [0], [0], [1])
+    assert st == 1
+    st, _ = _plan(gbla_lib, [0], [0], [129], [1])
+    assert st == 1
+    st, p = _plan(gbla_lib, [], [], [], [])
+    assert st == 0
+    assert gbla_lib.gbla_sposv_ragged(p, None, None, None, 1, stream()) == 0   # empty plan: no-op
+    assert gbla_lib.gbla_ragged_plan_destroy(p) == 0
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_d3_config_full_size(gbla_lib, cuda, dt):
+    """Config D3 at full size: 20000 systems, n log-uniform in [4,128], nrhs 1..8.
+    Every system: relative residual; a sample: the FP64 oracle at <= 1e-6."""
+    n, nrhs, a_off, b_off, A, B = workloads.d3_ragged(dtype=np.float64)
+    refine = 1 if dt == np.float32 else 2
+    _, X, info = _solve(gbla_lib, n, nrhs, a_off, b_off, A, B, dt, refine)
+    assert (info == 0).all()
+    idx = np.arange(0, len(n), 97)
+    sub = lambda arr, off, sz: np.concatenate([arr[off[i]:off[i] + sz[i]] for i in idx])
+    a_sz, b_sz = n.astype(np.int64) ** 2, n.astype(np.int64) * nrhs
+    As, Bs = sub(A, a_off, a_sz), sub(B, b_off, b_sz)
+    a2 = np.concatenate([[0], np.cumsum(a_sz[idx])[:-1]]); b2 = np.concatenate([[0], np.cumsum(b_sz[idx])[:-1]])
+    _, Xo, _ = O.posv_ragged(As.astype(dt), Bs.astype(dt), a2, b2, n[idx], nrhs[idx])
+    Xs = sub(X, b_off, b_sz)
+    assert _max_rel_err(n[idx], nrhs[idx], b2, Xs, Xo) < 1e-6
+    worst = 0.0
+    for i in range(0, len(n), 13):
+        k, r = n[i], nrhs[i]
+        M = A[a_off[i]:a_off[i] + k * k].reshape(k, k).T
+        b = B[b_off[i]:b_off[i] + k * r].reshape(r, k).T
+        x = X[b_off[i]:b_off[i] + k * r].reshape(r, k).T.astype(np.float64)
+        worst = max(worst, np.linalg.norm(M @ x - b) / np.linalg.norm(b))
+    assert worst < 1e-6
