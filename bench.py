@@ -43,6 +43,8 @@ import numpy as np  # noqa: E402
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic.json")
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+# FP32 FFMA rate measured on this GB300 with gbla_diag_fma_throughput (profiles/peaks_fma.md)
+FFMA_TFLOPS = 77.96
 
 # algorithmic work per unit (each input read once, each output written once)
 GEMM_BYTES_PER_PAIR = 3 * 64 * 64 * 4                       # A, B in; C out
@@ -59,11 +61,15 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["d2", "d1"], default="d2")
+    ap.add_argument("--workload", choices=["d2", "d1", "d3", "d4", "d5"], default="d2")
+    ap.add_argument("--dtype", choices=["f32", "f64"], default="f32", help="data type of the ragged workload d3")
+    ap.add_argument("--ref-sample", type=int, default=0,
+                    help="matrices the reference SVD host loop runs on (d4/d5; scaled to the batch)")
     ap.add_argument("--refine", type=int, default=1, help="least-squares refinement steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-library", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--peaks", action="store_true", help="print the measured FFMA / DFMA rates and exit")
     return ap.parse_args(argv)
 
 
@@ -230,6 +236,48 @@ def cpu_baseline_d1(seconds: float):
             "sample": f"{calls} x 4096 16x16 Cholesky factor+solve in {t:.1f} s (FP64, OpenMP over matrices)"}
 
 
+def _ragged_subset(count, seed, dtype):
+    from gputils_gb300 import workloads
+    return workloads.d3_ragged(count=count, seed=seed, dtype=dtype)
+
+
+def cpu_baseline_d3(seconds: float, dtype=np.float32):
+    """FP64 potrf + potrs per system (OpenMP over systems) on a 2000-system
+    sample of the ragged distribution; systems/s."""
+    from oracle import oracle as O
+
+    O.set_threads(os.cpu_count() or 1)
+    n, nrhs, a_off, b_off, A, B = _ragged_subset(2000, 31, np.float64)
+    calls, t = _repeat_timed(lambda: O.posv_ragged(A, B, a_off, b_off, n, nrhs), seconds)
+    return {"value": 2000 * calls / t, "unit": "matrices/s", "cores": O.max_threads(), "kind": "port",
+            "sample": f"{calls} x 2000 ragged SPD systems (n 4..128, nrhs 1..8) in {t:.1f} s "
+                      f"(FP64 potrf + potrs per system, OpenMP over systems)"}
+
+
+def cpu_baseline_svd(seconds: float, n: int):
+    """FP64 one-sided Jacobi SVD per matrix (OpenMP over matrices) on a
+    sample of the parametric family; matrices/s."""
+    from gputils_gb300 import workloads
+    from oracle import oracle as O
+
+    O.set_threads(os.cpu_count() or 1)
+    k = 256 if n <= 32 else 64
+    A = workloads.svd_family(k, n, seed=41)[0]
+    calls, t = _repeat_timed(lambda: O.gesvj(A, tol=1e-6), seconds)
+    return {"value": k * calls / t, "unit": "matrices/s", "cores": O.max_threads(), "kind": "port",
+            "sample": f"{calls} x {k} {n}x{n} one-sided Jacobi SVDs (FP64, tol 1e-6) in {t:.1f} s "
+                      f"(OpenMP over matrices)"}
+
+
+CPU_BASELINES = {
+    "d1": lambda sec, args: cpu_baseline_d1(sec),
+    "d2": lambda sec, args: cpu_baseline_d2(sec),
+    "d3": lambda sec, args: cpu_baseline_d3(sec),
+    "d4": lambda sec, args: cpu_baseline_svd(sec, 32),
+    "d5": lambda sec, args: cpu_baseline_svd(sec, 64),
+}
+
+
 # ------------------------------------------------------------ reference arm
 def run_reference_arm(args):
     rank, world, _ = dist_env()
@@ -240,17 +288,17 @@ def run_reference_arm(args):
             return
     # each step is a bounded sample: about cpu_seconds, and the whole run a few minutes at most
     budget = max(0.5, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
-    fn = cpu_baseline_d2 if args.workload == "d2" else cpu_baseline_d1
+    fn = CPU_BASELINES[args.workload]
     for _ in range(args.warmup):
-        fn(min(budget, 2.0))
-    vals = [fn(budget) for _ in range(args.steps)]
+        fn(min(budget, 2.0), args)
+    vals = [fn(budget, args) for _ in range(args.steps)]
     v = statistics.median([x["value"] for x in vals])
     first = vals[0]
     line = {
         "impl": "reference", "metric": metric_name(args.workload), "value": v, "unit": "matrices/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": workload_config(args.workload),
+        "config": workload_config(args.workload, args),
         "cpu_baseline": {"value": v, "unit": "matrices/s", "cores": first["cores"], "kind": first["kind"],
                          "sample": first["sample"]},
         "e2e": {"value": v, "unit": "matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -265,15 +313,28 @@ def metric_name(workload):
     return "matrices/s on 1 GB300 (Chol/QR/SVD batched) vs ref cuSOLVER build at equal FP64 err"
 
 
-def workload_config(workload):
+def workload_config(workload, args=None):
     if workload == "d2":
         return {"workload": "precision: addAB 16384 x 64x64x64 fp32 (BF16x6 tcgen05) + leastSquaresBatched "
                             "8192 x 128x32 fp32, 4 RHS, kappa 1e3 (FP32 QR + double-FP32 refinement)",
                 "gemm_pairs": 16384, "ls_systems": 8192, "parallelism": "replicas",
                 "l2": "inputs larger than L2 every step (per-step copies of the least-squares inputs)"}
-    return {"workload": "Cholesky factor+solve 4096 x 16x16 fp32, 1 RHS (CholeskyBatchFactoriser API: potrf + potrs)",
-            "matrices": 4096, "parallelism": "replicas",
-            "l2": "L2 flushed between timed steps (the 4.5 MB working set fits in L2)"}
+    if workload == "d1":
+        return {"workload": "Cholesky factor+solve 4096 x 16x16 fp32, 1 RHS (CholeskyBatchFactoriser API: potrf + potrs)",
+                "matrices": 4096, "parallelism": "replicas",
+                "l2": "L2 flushed between timed steps (the 4.5 MB working set fits in L2)"}
+    if workload == "d3":
+        dt = getattr(args, "dtype", "f32") if args is not None else "f32"
+        return {"workload": f"ragged Cholesky factor+solve, 20000 SPD systems, n log-uniform in [4,128], "
+                            f"nrhs 1..8, {dt}, one call (plan + CUDA graph), FP32 factor + refinement",
+                "systems": 20000, "dtype": dt, "parallelism": "replicas",
+                "l2": "inputs larger than L2 every step (per-step copies of the arenas)"}
+    n = 32 if workload == "d4" else 64
+    k = 8192 if workload == "d4" else 32768
+    return {"workload": f"one-sided Jacobi SVD (Svd::factorise, S and V^T) of {k} {n}x{n} fp32 matrices of the "
+                        f"parametric family A0 + sum theta_j A_j, tol 1e-6, cold start",
+            "matrices": k, "n": n, "parallelism": "replicas",
+            "l2": "per-step copies of the input (the SVD destroys it)"}
 
 
 # ------------------------------------------------------------- ours: d2
@@ -291,6 +352,10 @@ class RefLib:
         self.L.refp_sgels_batched.argtypes = [ip, ip, vp, vp, ip, vp]
         self.L.refp_spotrf_batched.argtypes = [ip, vp, vp, ip]
         self.L.refp_spotrs_batched.argtypes = [ip, vp, vp, vp, ip]
+        self.L.refp_dpotrf_batched.argtypes = [ip, vp, vp, ip]
+        self.L.refp_dpotrs_batched.argtypes = [ip, vp, vp, vp, ip]
+        self.L.refp_sgesvd_lwork.argtypes = [ip, ip]
+        self.L.refp_sgesvd_loop.argtypes = [ip, ip, vp, vp, vp, vp, vp, ip, vp, ip, ip]
         assert self.L.refp_init(stream) == 0
 
 
@@ -415,7 +480,7 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_max / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded numpy generators, configuration distributions)",
-        "config": dict(workload_config("d2"), refine_steps=args.refine),
+        "config": dict(workload_config("d2", args), refine_steps=args.refine),
         "roofline": dict(rl[dom], kernel=dom),
         "roofline_all": rl,
         "max_rel_err_vs_fp64": {"gemm": err_gemm, "least_squares_x": err_ls},
@@ -485,6 +550,291 @@ def reference_library_d2(dev, st, Ag, Bg, Cg, LA0, LB0, A, B, LA, LB):
                      "(one call; nrhs = 1 in the reference API)"}
 
 
+# ------------------------------------------------------------- ours: d3
+def _ragged_bytes(n, nrhs, elem):
+    n = n.astype(np.int64)
+    return int((elem * (n * n + n * (n + 1) // 2 + 2 * n * nrhs)).sum())
+
+
+def run_ours_d3(args, dev, st, L, rank, world, dist):
+    """One gbla_{s,d}posv_ragged call per step on 20000 mixed systems,
+    captured once per step buffer in a CUDA graph and replayed."""
+    import torch
+    from gputils_gb300 import workloads, _lib
+    from oracle import oracle as O
+
+    dt = np.float32 if args.dtype == "f32" else np.float64
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    n, nrhs, a_off, b_off, A, B = workloads.d3_ragged(dtype=dt)
+    count = len(n)
+    plan = C.c_void_p()
+    _lib.check(L.gbla_ragged_plan_create(np.ascontiguousarray(a_off).ctypes.data,
+                                         np.ascontiguousarray(b_off).ctypes.data,
+                                         np.ascontiguousarray(n, np.int32).ctypes.data,
+                                         np.ascontiguousarray(nrhs, np.int32).ctypes.data, count, C.byref(plan)),
+               "plan")
+    refine = 1 if dt == np.float32 else 2
+    fn = L.gbla_sposv_ragged if dt == np.float32 else L.gbla_dposv_ragged
+    A0 = torch.from_numpy(A).to(dev)
+    B0 = torch.from_numpy(B).to(dev)
+    nsteps = args.warmup + args.steps
+    As = [A0.clone() for _ in range(nsteps)]
+    Bs = [B0.clone() for _ in range(nsteps)]
+    info = torch.empty(count, dtype=torch.int32, device=dev)
+    # one CUDA graph per step buffer (each replay is the whole ragged solve)
+    graphs = []
+    cap = torch.cuda.Stream()
+    for i in range(nsteps):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=cap):
+            cs = torch.cuda.current_stream().cuda_stream
+            _lib.check(fn(plan, As[i].data_ptr(), Bs[i].data_ptr(), info.data_ptr(), refine, cs), "posv_ragged")
+        graphs.append(g)
+    torch.cuda.synchronize()
+    # graph capture recorded the work but did not run it: restore pristine inputs
+    for i in range(nsteps):
+        As[i].copy_(A0); Bs[i].copy_(B0)
+    torch.cuda.synchronize()
+    for i in range(args.warmup):
+        graphs[i].replay()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        e0.record()
+        for i in range(args.steps):
+            graphs[args.warmup + i].replay()
+        e1.record()
+        torch.cuda.synchronize()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    elapsed_max, units_all = aggregate(elapsed, count * args.steps, world, dist, dev)
+    assert (info.cpu().numpy() == 0).all()
+    # accuracy vs FP64 on a sample of systems
+    X = Bs[args.warmup].cpu().numpy()
+    idx = np.arange(0, count, 41)
+    a_sz, b_sz = n.astype(np.int64) ** 2, n.astype(np.int64) * nrhs
+    As_ = np.concatenate([A[a_off[i]:a_off[i] + a_sz[i]] for i in idx])
+    Bs_ = np.concatenate([B[b_off[i]:b_off[i] + b_sz[i]] for i in idx])
+    a2 = np.concatenate([[0], np.cumsum(a_sz[idx])[:-1]]); b2 = np.concatenate([[0], np.cumsum(b_sz[idx])[:-1]])
+    _, Xo, _ = O.posv_ragged(As_, Bs_, a2, b2, n[idx], nrhs[idx])
+    err = 0.0
+    for j, i in enumerate(idx):
+        x = X[b_off[i]:b_off[i] + b_sz[i]].astype(np.float64)
+        xo = Xo[b2[j]:b2[j] + b_sz[i]]
+        err = max(err, float(np.linalg.norm(x - xo) / np.linalg.norm(xo)))
+
+    # e2e: pinned host arenas, H2D of A and B, the solve, D2H of X, per step
+    hA, hB = torch.from_numpy(A).pin_memory(), torch.from_numpy(B).pin_memory()
+    hX = torch.empty_like(hB).pin_memory()
+    dA, dB = torch.empty_like(A0), torch.empty_like(B0)
+
+    def e2e_step():
+        dA.copy_(hA, non_blocking=True); dB.copy_(hB, non_blocking=True)
+        _lib.check(fn(plan, dA.data_ptr(), dB.data_ptr(), info.data_ptr(), refine, st), "posv_ragged")
+        hX.copy_(dB, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    esteps = max(3, min(args.steps, 10))
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(esteps):
+        e2e_step()
+    f1.record()
+    torch.cuda.synchronize()
+    e2e_t, _ = aggregate(f0.elapsed_time(f1) / 1e3 / esteps, 0.0, world, dist, dev)
+
+    reflib = None
+    if not args.no_reference_library:
+        try:
+            reflib = reference_library_d3(dev, st, n, nrhs, a_off, b_off, A0, B0, dt)
+        except Exception as exc:
+            reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
+    _lib.check(L.gbla_ragged_plan_destroy(plan), "plan destroy")
+    pk = peaks()
+    t = elapsed_max / args.steps
+    bytes_ = _ragged_bytes(n, nrhs, np.dtype(dt).itemsize)
+    ach = bytes_ / t / 1e9
+    launches = 4 if dt == np.float32 else 4
+    return {
+        "metric": metric_name("d3"), "value": units_all / elapsed_max, "unit": "matrices/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded)",
+        "config": dict(workload_config("d3", args), refine_steps=refine),
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach / pk["hbm_gbs"], "traffic": traffic_for("ragged_d3_" + args.dtype),
+                     "kernel": "posv_ragged (all kernels of one call)", "algorithmic_bytes_per_launch": bytes_},
+        "max_rel_err_vs_fp64": {"x": err},
+        "e2e": {"value": count * world / e2e_t, "unit": "matrices/s",
+                "h2d_bytes_per_step": int(hA.numel() + hB.numel()) * hA.element_size(),
+                "d2h_bytes_per_step": int(hX.numel()) * hX.element_size(), "ms_per_step": e2e_t * 1e3},
+        "gpu_launches": launches * args.steps, "clocks": clk.summary(), "reference_library": reflib,
+    }
+
+
+def reference_library_d3(dev, st, n, nrhs, a_off, b_off, A0, B0, dt):
+    """The reference's way to solve a ragged batch: for each distinct n one
+    potrfBatched over that size group (CholeskyBatchFactoriser::factorise),
+    then one potrsBatched per right-hand-side column (solve takes nrhs = 1),
+    over the systems that have that column.  Pointer arrays address the
+    matrices in place (no gathers)."""
+    import torch
+    from oracle import oracle as O
+
+    R = RefLib(st)
+    elem = np.dtype(dt).itemsize
+    calls = []
+    for nn in np.unique(n):
+        ids = np.nonzero(n == nn)[0]
+        pa = torch.tensor(A0.data_ptr() + a_off[ids] * elem, dtype=torch.int64, device=dev)
+        info = torch.zeros(len(ids), dtype=torch.int32, device=dev)
+        calls.append(("f", int(nn), pa, None, info, len(ids)))
+        for c in range(int(nrhs[ids].max())):
+            sel = ids[nrhs[ids] > c]
+            pl = torch.tensor(A0.data_ptr() + a_off[sel] * elem, dtype=torch.int64, device=dev)
+            pb = torch.tensor(B0.data_ptr() + (b_off[sel] + c * nn) * elem, dtype=torch.int64, device=dev)
+            calls.append(("s", int(nn), pl, pb, info, len(sel)))
+    potrf = R.L.refp_spotrf_batched if dt == np.float32 else R.L.refp_dpotrf_batched
+    potrs = R.L.refp_spotrs_batched if dt == np.float32 else R.L.refp_dpotrs_batched
+    Ac, Bc = A0.clone(), B0.clone()
+
+    def run():
+        for kind, nn, p1, p2, info, k in calls:
+            if kind == "f":
+                assert potrf(nn, p1.data_ptr(), info.data_ptr(), k) == 0
+            else:
+                assert potrs(nn, p1.data_ptr(), p2.data_ptr(), info.data_ptr(), k) == 0
+
+    run()
+    torch.cuda.synchronize()
+    reps, tot = 3, 0.0
+    for _ in range(reps):
+        A0.copy_(Ac); B0.copy_(Bc)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        e[0].record(); run(); e[1].record()
+        torch.cuda.synchronize()
+        tot += e[0].elapsed_time(e[1]) / 1e3
+    t = tot / reps
+    X = B0.cpu().numpy()
+    A0.copy_(Ac); B0.copy_(Bc)
+    idx = np.arange(0, len(n), 41)
+    err = 0.0
+    Ah, Bh = Ac.cpu().numpy(), Bc.cpu().numpy()
+    for i in idx:
+        k, r = int(n[i]), int(nrhs[i])
+        M = Ah[a_off[i]:a_off[i] + k * k].reshape(k, k).T.astype(np.float64)
+        b = Bh[b_off[i]:b_off[i] + k * r].reshape(r, k).T.astype(np.float64)
+        xo = np.linalg.solve(M, b)
+        x = X[b_off[i]:b_off[i] + k * r].reshape(r, k).T
+        err = max(err, float(np.linalg.norm(x - xo) / np.linalg.norm(xo)))
+    return {"value": len(n) / t, "unit": "matrices/s", "ms": t * 1e3, "library_calls": len(calls),
+            "max_rel_err_vs_fp64": {"x": err},
+            "calls": "per size n: cusolverDn<t>potrfBatched, then per RHS column cusolverDn<t>potrsBatched "
+                     "(nrhs = 1) over the systems having that column"}
+
+
+# ------------------------------------------------------------- ours: d4 / d5
+def run_ours_svd(args, dev, st, L, rank, world, dist):
+    import torch
+    from gputils_gb300 import workloads, _lib
+    from oracle import oracle as O
+
+    nmat = 32 if args.workload == "d4" else 64
+    Ah = workloads.d4_svd32() if args.workload == "d4" else workloads.d5_svd64()
+    k = Ah.shape[0]
+    A0 = to_dev(Ah, dev)
+    nsteps = args.warmup + args.steps
+    As = [A0.clone() for _ in range(nsteps)]
+    S = torch.empty(k * nmat, dtype=torch.float32, device=dev)
+    Vt = torch.empty(k * nmat * nmat, dtype=torch.float32, device=dev)
+    info = torch.empty(k, dtype=torch.int32, device=dev)
+    sweeps = torch.empty(k, dtype=torch.int32, device=dev)
+
+    def step(i):
+        _lib.check(L.gbla_sgesvj_batched(nmat, nmat, As[i].data_ptr(), nmat * nmat, S.data_ptr(), nmat,
+                                         Vt.data_ptr(), nmat * nmat, None, 0, None, 0, 1e-6, 60,
+                                         info.data_ptr(), sweeps.data_ptr(), k, st), "gesvj")
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        e0.record()
+        for i in range(args.steps):
+            step(args.warmup + i)
+        e1.record()
+        torch.cuda.synchronize()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    elapsed_max, units_all = aggregate(elapsed, k * args.steps, world, dist, dev)
+    assert (info.cpu().numpy() == 0).all()
+    sw = sweeps.cpu().numpy()
+    idx = np.arange(0, k, 64 if nmat == 32 else 512)
+    Sh = S.cpu().numpy().reshape(k, nmat)
+    So = O.gesvj(Ah[idx], tol=1e-12)["S"]
+    err = rel_err(Sh[idx][:, None, :], So[:, None, :])
+    reflib = None
+    if not args.no_reference_library:
+        try:
+            reflib = reference_library_svd(dev, st, A0, Ah, nmat, args.ref_sample or (512 if nmat == 32 else 128))
+        except Exception as exc:
+            reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
+    pk = peaks()
+    t = elapsed_max / args.steps
+    flops = (4 * nmat ** 3 + 8 * nmat ** 3) * k
+    return {
+        "metric": metric_name(args.workload), "value": units_all / elapsed_max, "unit": "matrices/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded parametric family)", "config": workload_config(args.workload, args),
+        "roofline": {"bound": "fp32 cuda cores", "achieved": flops / t / 1e12, "peak": FFMA_TFLOPS,
+                     "unit": "TFLOP/s", "frac": flops / t / 1e12 / FFMA_TFLOPS, "traffic": None,
+                     "kernel": "gesvj", "algorithmic_flops_per_launch": flops,
+                     "peak_source": "measured FFMA rate (gbla_diag_fma_throughput)"},
+        "max_rel_err_vs_fp64": {"sigma": err}, "sweeps": {"mean": float(sw.mean()), "max": int(sw.max())},
+        "gpu_launches": args.steps, "clocks": clk.summary(), "reference_library": reflib, "e2e": None,
+    }
+
+
+def reference_library_svd(dev, st, A0, Ah, nmat, sample):
+    """Svd<float>::factorise: a host loop of cusolverDnSgesvd('N', 'A') over the
+    matrices; timed on the first `sample` matrices and scaled (the loop's cost
+    is linear in the matrix count)."""
+    import torch
+    from oracle import oracle as O
+
+    R = RefLib(st)
+    lwork = R.L.refp_sgesvd_lwork(nmat, nmat)
+    assert lwork >= 0
+    work = torch.empty(max(lwork, 1), dtype=torch.float32, device=dev)
+    Ac = A0[:sample].clone()
+    S = torch.empty(sample * nmat, dtype=torch.float32, device=dev)
+    Vt = torch.empty(sample * nmat * nmat, dtype=torch.float32, device=dev)
+    info = torch.empty(sample, dtype=torch.int32, device=dev)
+
+    def run():
+        assert R.L.refp_sgesvd_loop(nmat, nmat, Ac.data_ptr(), S.data_ptr(), None, Vt.data_ptr(), work.data_ptr(),
+                                    lwork, info.data_ptr(), sample, 0) == 0
+
+    Ac.copy_(A0[:sample]); run(); torch.cuda.synchronize()
+    Ac.copy_(A0[:sample])
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    e[0].record(); run(); e[1].record()
+    torch.cuda.synchronize()
+    t = e[0].elapsed_time(e[1]) / 1e3
+    So = O.gesvj(Ah[:min(sample, 64)], tol=1e-12)["S"]
+    err = rel_err(S.cpu().numpy().reshape(sample, nmat)[:len(So)][:, None, :], So[:, None, :])
+    return {"value": sample / t, "unit": "matrices/s", "sample": sample, "ms_for_sample": t * 1e3,
+            "max_rel_err_vs_fp64": {"sigma": err},
+            "calls": f"host loop of cusolverDnSgesvd('N','A'), {sample} calls timed, scaled linearly"}
+
+
 def run_ours_d1(args, dev, st, L, rank, world, dist):
     """CholeskyBatchFactoriser factorise() + solve() on 4096 16x16: the
     reference API path (2 launches: potrf, potrs)."""
@@ -521,6 +871,32 @@ def run_ours_d1(args, dev, st, L, rank, world, dist):
     idx = np.arange(0, k, 16)
     _, xo, _ = O.posv(M[idx], b[idx])
     err = rel_err(x[idx], xo)
+    reflib = None
+    if not args.no_reference_library:
+        try:
+            R = RefLib(st)
+            Mr, br = to_dev(M, dev), to_dev(b, dev)
+            pa, pb = ptr_array(Mr, k, n * n, dev), ptr_array(br, k, n, dev)
+            rinfo = torch.empty(k, dtype=torch.int32, device=dev)
+            M0, b0 = Mr.clone(), br.clone()
+            tt = []
+            for rep in range(args.warmup + args.steps):
+                Mr.copy_(M0); br.copy_(b0); flush.zero_()
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                torch.cuda.synchronize()
+                e[0].record()
+                assert R.L.refp_spotrf_batched(n, pa.data_ptr(), rinfo.data_ptr(), k) == 0
+                assert R.L.refp_spotrs_batched(n, pa.data_ptr(), pb.data_ptr(), rinfo.data_ptr(), k) == 0
+                e[1].record()
+                torch.cuda.synchronize()
+                if rep >= args.warmup:
+                    tt.append(e[0].elapsed_time(e[1]) / 1e3)
+            xr = from_dev(br, k, n, 1)
+            reflib = {"value": k / (sum(tt) / len(tt)), "unit": "matrices/s", "ms": sum(tt) / len(tt) * 1e3,
+                      "max_rel_err_vs_fp64": {"x": rel_err(xr[idx], xo)},
+                      "calls": "cusolverDnSpotrfBatched + cusolverDnSpotrsBatched (nrhs = 1)"}
+        except Exception as exc:
+            reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
     pk = peaks()
     bytes_ = 4 * (n * n + n * (n + 1) // 2 + 2 * n) * k
     t = elapsed / args.steps
@@ -529,16 +905,32 @@ def run_ours_d1(args, dev, st, L, rank, world, dist):
         "metric": metric_name("d1"), "value": units_all / elapsed_max, "unit": "matrices/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_max / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)", "config": workload_config("d1"),
+        "data": "synthetic (seeded)", "config": workload_config("d1", args),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": ach / pk["hbm_gbs"], "traffic": traffic_for("chol_d1"), "kernel": "potrf+potrs"},
         "max_rel_err_vs_fp64": {"x": err}, "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
-        "e2e": None,
+        "e2e": None, "reference_library": reflib,
     }
+
+
+def print_peaks():
+    from gputils_gb300 import build, _lib
+
+    build.build_lib()
+    L = _lib.lib()
+    out = {}
+    for prec, iters in ((32, 20000), (64, 200)):
+        g, ms = C.c_double(), C.c_double()
+        _lib.check(L.gbla_diag_fma_throughput(prec, iters, C.byref(g), C.byref(ms)), "diag")
+        out[f"fp{prec}_fma_tflops"] = g.value / 1e3
+    print(json.dumps(out), flush=True)
 
 
 def main(argv=None):
     args = parse_args(argv)
+    if args.peaks:
+        print_peaks()
+        return
     if args.impl == "reference":
         run_reference_arm(args)
         return
@@ -555,12 +947,9 @@ def main(argv=None):
         dist.barrier()
     L = _lib.lib()
     st = torch.cuda.current_stream().cuda_stream
-    if args.workload == "d2":
-        line = run_ours_d2(args, dev, st, L, rank, world, dist)
-        cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline_d2(args.cpu_seconds)
-    else:
-        line = run_ours_d1(args, dev, st, L, rank, world, dist)
-        cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline_d1(args.cpu_seconds)
+    runners = {"d1": run_ours_d1, "d2": run_ours_d2, "d3": run_ours_d3, "d4": run_ours_svd, "d5": run_ours_svd}
+    line = runners[args.workload](args, dev, st, L, rank, world, dist)
+    cpu = None if args.no_cpu_baseline or rank != 0 else CPU_BASELINES[args.workload](args.cpu_seconds, args)
     line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
