@@ -8,7 +8,10 @@
 // (p < q) is rotated when |a_p . a_q| > tol ||a_p|| ||a_q|| with the
 // Rutishauser formulas (zeta = (|a_q|^2 - |a_p|^2) / (2 a_p.a_q),
 // t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2))); the sweep loop ends after a
-// sweep without rotations or after max_sweeps (info = 1 then).
+// sweep without rotations or after max_sweeps (info = 1 then).  Columns
+// stored in FP32 cannot be orthogonal to better than about sqrt(m) u
+// (u = 2^-24) relative, so the tolerance used is max(tol, 4 sqrt(m) u);
+// below it a rotation would only stir rounding noise.
 //
 // Two kernel shapes:
 //  * n <= 32, m <= 64 : one warp per matrix, lane j owns column j of A and of
@@ -50,6 +53,12 @@ __device__ __forceinline__ bool jacobi_rotation(float alpha, float beta, float g
     c = 1.f / sqrtf(fmaf(t, t, 1.f));
     s = c * t;
     return true;
+}
+
+// Tolerance actually used: the request, but not below the FP32 noise floor
+// of |a_p . a_q| / (|a_p| |a_q|) for m-row columns.
+__device__ __forceinline__ float jacobi_tol(float tol, int m) {
+    return fmaxf(tol, 4.f * sqrtf((float)m) * 5.9604645e-8f);
 }
 
 // ----------------------------------------------------------- warp kernel
@@ -95,6 +104,7 @@ __global__ void __launch_bounds__(128, 1)
 #pragma unroll
     for (int i = 0; i < MR; i++) fro2 = fmaf(a[i], a[i], fro2);
     const float small = FLT_EPSILON * FLT_EPSILON * warp_sum(fro2);
+    tol = jacobi_tol(tol, m);
 
     int sweep = 0, converged = 0;
     for (sweep = 1; sweep <= max_sweeps; sweep++) {
@@ -240,7 +250,6 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
     float *v = a + (size_t)n * lda;       // n columns x ldv
     float *sig = v + (size_t)n * ldv;     // n
     float *rinv = sig + n;                // n: 1 / |rotated column j|
-    __shared__ int s_flag;
     const int tid = threadIdx.x, g = tid / SVJ_GROUP, gl = tid % SVJ_GROUP;
     const int N = n + (n & 1), M = N - 1;
 
@@ -287,11 +296,10 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
         }
         __syncthreads();
         const float small = FLT_EPSILON * FLT_EPSILON * sig[0];
+        const float tol_eff = jacobi_tol(tol, m);
         __syncthreads();
         int sweep = 0, converged = 0;
         for (sweep = 1; sweep <= max_sweeps; sweep++) {
-            if (tid == 0) s_flag = 0;
-            __syncthreads();
             int rotated = 0;
             for (int r = 0; r < M; r++) {
                 int p = -1, q = -1;
@@ -315,7 +323,7 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
                 beta = group_sum(beta, SVJ_GROUP);
                 gamma = group_sum(gamma, SVJ_GROUP);
                 float c, s;
-                if (act && jacobi_rotation(alpha, beta, gamma, tol, small, c, s)) {
+                if (act && jacobi_rotation(alpha, beta, gamma, tol_eff, small, c, s)) {
                     rotated = 1;
                     for (int i = gl; i < m; i += SVJ_GROUP) {
                         float x = a[p * lda + i], y = a[q * lda + i];
@@ -330,9 +338,8 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
                 }
                 __syncthreads();
             }
-            if (rotated) s_flag = 1;
-            __syncthreads();
-            if (!s_flag) { converged = 1; break; }
+            // block-wide OR in one barrier: every thread sees the same decision
+            if (!__syncthreads_or(rotated)) { converged = 1; break; }
         }
         if (sweep > max_sweeps) sweep = max_sweeps;
         // ---- epilogue: normalise V; sigma_j = |A v_j| from the original A (see

@@ -177,7 +177,9 @@ gbla_status gbla_dgels_batched(int m, int n, int nrhs, double *A, int64_t stride
  * rightSingularVectors returns).  U_i: m x m, nullable (computeU = false).
  * A_i is destroyed (it ends as A_i V_i).  V0 (nullable): n x n orthogonal warm
  * start; A_i V0_i is orthogonalised and V starts at V0.  A pair of columns is
- * rotated while |a_p.a_q| > tol |a_p||a_q|; info[i] = 1 if max_sweeps sweeps
+ * rotated while |a_p.a_q| > tol' |a_p||a_q|, tol' = max(tol, 4 sqrt(m) 2^-24)
+ * (FP32 columns cannot be more orthogonal than that); singular values are
+ * recomputed as |A v_j| at the end.  info[i] = 1 if max_sweeps sweeps
  * did not converge (nullable), sweeps[i] = sweeps used (nullable).  Sign
  * rule: the largest-magnitude entry of each v_j is negative.
  * Replaces the host loop of cusolverDn<t>gesvd in Svd<T>::factorise

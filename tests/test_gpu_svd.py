@@ -167,3 +167,14 @@ def test_nullspace_random_rank_deficient(gbla_lib, cuda):
         assert np.abs(A[i] @ Ni).max() < 1e-4
         assert np.abs(Ni.T @ Ni - np.eye(nul[i])).max() < 1e-5
         assert np.abs(P[i] - Ni @ Ni.T).max() < 1e-5
+
+
+def test_d5_family_64_converges(gbla_lib, cuda):
+    """The 64x64 parametric family (config D5) on 1024 matrices: every matrix
+    converges, sigma within 1e-6 of FP64 on a sample."""
+    A = workloads.svd_family(1024, 64, seed=6)[0]
+    r = _svd(gbla_lib, A, tol=1e-6, max_sweeps=60)
+    assert (r["info"] == 0).all(), r["sweeps"].max()
+    idx = np.arange(0, 1024, 37)
+    o = O.gesvj(A[idx])
+    assert rel_err(r["S"][idx][:, None, :], o["S"][:, None, :]) < 1e-6
