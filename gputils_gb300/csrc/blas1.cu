@@ -99,6 +99,42 @@ static gbla_status copy_rows(int m, int n, int r0, int nr, const T *A, T *out, c
     return launch_status();
 }
 
+// ------------------------------------------------------------- Givens
+// x_i <- c x_i + s y_i,  y_i <- c y_i - s x_i  (cublas<t>rot semantics); c and
+// s come either by value or from device memory (cs != nullptr: c = cs[0],
+// s = cs[1]) so a rotation computed on the device needs no host round trip.
+template <typename T>
+__global__ void k_rot(int64_t len, T *__restrict__ x, int64_t incx, T *__restrict__ y, int64_t incy, T c, T s,
+                      const T *__restrict__ cdev, const T *__restrict__ sdev) {
+    if (cdev) { c = *cdev; s = *sdev; }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+        T xv = x[i * incx], yv = y[i * incy];
+        x[i * incx] = c * xv + s * yv;
+        y[i * incy] = c * yv - s * xv;
+    }
+}
+
+template <typename T>
+static gbla_status rot(int64_t len, T *x, int64_t incx, T *y, int64_t incy, T c, T s, const T *cdev, const T *sdev,
+                       cudaStream_t st) {
+    if (len < 0 || incx < 1 || incy < 1) return GBLA_INVALID_VALUE;
+    if (len == 0) return GBLA_SUCCESS;
+    if (!x || !y || (cdev == nullptr) != (sdev == nullptr)) return GBLA_INVALID_VALUE;
+    k_rot<T><<<stream_grid(len), 256, 0, st>>>(len, x, incx, y, incy, c, s, cdev, sdev);
+    return launch_status();
+}
+
+// out[0] = 1 / hypot(a_ij, a_kj), out[1] = a_ij out[0], out[2] = a_kj out[0]:
+// the rotation of rows i and k that zeroes a_kj (GivensAnnihilator).
+template <typename T>
+__global__ void k_givens_coeffs(const T *__restrict__ A, int64_t ld, int i, int k, int j, T *__restrict__ out) {
+    const T xi = A[(int64_t)j * ld + i], xk = A[(int64_t)j * ld + k];
+    const T r = rhypot(xi, xk);
+    out[0] = r;
+    out[1] = xi * r;
+    out[2] = xk * r;
+}
+
 // --------------------------------------------------------------- reductions
 // Pass 1: a fixed number of blocks (depending only on len) each reduce a
 // grid-strided slice into one partial; pass 2: one block reduces the
@@ -289,5 +325,36 @@ GBLA_API gbla_status gbla_sdot_noalloc(int64_t len, const float *x, const float 
     s = launch_status();
     if (s != GBLA_SUCCESS) return s;
     k_reduce_pass2<float, RED_DOT><<<1, RED_THREADS, 0, st>>>(nb, parts, result);
+    return launch_status();
+}
+
+GBLA_API gbla_status gbla_srot(int64_t len, float *x, int64_t incx, float *y, int64_t incy, float c, float s,
+                               cudaStream_t st) {
+    return rot<float>(len, x, incx, y, incy, c, s, nullptr, nullptr, st);
+}
+GBLA_API gbla_status gbla_drot(int64_t len, double *x, int64_t incx, double *y, int64_t incy, double c, double s,
+                               cudaStream_t st) {
+    return rot<double>(len, x, incx, y, incy, c, s, nullptr, nullptr, st);
+}
+GBLA_API gbla_status gbla_srot_dev(int64_t len, float *x, int64_t incx, float *y, int64_t incy, const float *c,
+                                   const float *s, cudaStream_t st) {
+    if (!c || !s) return GBLA_INVALID_VALUE;
+    return rot<float>(len, x, incx, y, incy, 0.f, 0.f, c, s, st);
+}
+GBLA_API gbla_status gbla_drot_dev(int64_t len, double *x, int64_t incx, double *y, int64_t incy, const double *c,
+                                   const double *s, cudaStream_t st) {
+    if (!c || !s) return GBLA_INVALID_VALUE;
+    return rot<double>(len, x, incx, y, incy, 0.0, 0.0, c, s, st);
+}
+GBLA_API gbla_status gbla_sgivens_coeffs(const float *A, int64_t ld, int i, int k, int j, float *out,
+                                         cudaStream_t st) {
+    if (!A || !out || i < 0 || k < 0 || j < 0 || i >= ld || k >= ld) return GBLA_INVALID_VALUE;
+    k_givens_coeffs<float><<<1, 1, 0, st>>>(A, ld, i, k, j, out);
+    return launch_status();
+}
+GBLA_API gbla_status gbla_dgivens_coeffs(const double *A, int64_t ld, int i, int k, int j, double *out,
+                                         cudaStream_t st) {
+    if (!A || !out || i < 0 || k < 0 || j < 0 || i >= ld || k >= ld) return GBLA_INVALID_VALUE;
+    k_givens_coeffs<double><<<1, 1, 0, st>>>(A, ld, i, k, j, out);
     return launch_status();
 }

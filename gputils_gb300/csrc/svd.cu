@@ -42,56 +42,64 @@ __device__ __forceinline__ int rr_partner(int i, int r, int N) {
 // Columns whose squared norm is <= small (FLT_EPSILON^2 |A|_F^2) are treated as
 // zero.  c and s use correctly rounded division and square root: rsqrt's
 // one-sided error would shrink the column norms over many rotations.
-__device__ __forceinline__ bool jacobi_rotation(float alpha, float beta, float gamma, float tol, float small, float &c,
-                                                float &s) {
-    if (alpha <= small || beta <= small || gamma == 0.f) return false;
-    if (!(fabsf(gamma) > tol * sqrtf(alpha) * sqrtf(beta))) return false;
-    const float zeta = (beta - alpha) / (2.f * gamma);
-    const float az = fabsf(zeta);
-    const float t = az < 1e18f ? copysignf(1.f, zeta) / (az + sqrtf(fmaf(zeta, zeta, 1.f))) : 0.5f / zeta;
-    if (t == 0.f) return false;
-    c = 1.f / sqrtf(fmaf(t, t, 1.f));
+template <typename T>
+__device__ __forceinline__ bool jacobi_rotation(T alpha, T beta, T gamma, T tol, T small, T &c, T &s) {
+    if (alpha <= small || beta <= small || gamma == T(0)) return false;
+    if (!(fabs(gamma) > tol * sqrt(alpha) * sqrt(beta))) return false;
+    const T zeta = (beta - alpha) / (T(2) * gamma);
+    const T az = fabs(zeta);
+    const T big = sizeof(T) == 4 ? T(1e18) : T(1e150);
+    const T t = az < big ? copysign(T(1), zeta) / (az + sqrt(fma(zeta, zeta, T(1)))) : T(0.5) / zeta;
+    if (t == T(0)) return false;
+    c = T(1) / sqrt(fma(t, t, T(1)));
     s = c * t;
     return true;
 }
 
+template <typename T> __device__ __forceinline__ T unit_roundoff();
+template <> __device__ __forceinline__ float unit_roundoff<float>() { return 5.9604645e-8f; }
+template <> __device__ __forceinline__ double unit_roundoff<double>() { return 1.1102230246251565e-16; }
+template <typename T> __device__ __forceinline__ T mach_eps() { return T(2) * unit_roundoff<T>(); }
+
 // Tolerance actually used: the request, but not below the FP32 noise floor
 // of |a_p . a_q| / (|a_p| |a_q|) for m-row columns.
-__device__ __forceinline__ float jacobi_tol(float tol, int m) {
-    return fmaxf(tol, 4.f * sqrtf((float)m) * 5.9604645e-8f);
+template <typename T>
+__device__ __forceinline__ T jacobi_tol(T tol, int m) {
+    const T floor_ = T(4) * sqrt(T(m)) * unit_roundoff<T>();
+    return tol > floor_ ? tol : floor_;
 }
 
 // ----------------------------------------------------------- warp kernel
-template <int MR>
+template <typename T, int MR>
 __global__ void __launch_bounds__(128, 1)
-    k_gesvj_warp(int m, int n, float *__restrict__ A, int64_t sA, float *__restrict__ S, int64_t sS,
-                 float *__restrict__ Vt, int64_t sVt, float *__restrict__ U, int64_t sU, const float *__restrict__ V0,
-                 int64_t sV0, float tol, int max_sweeps, int *__restrict__ info, int *__restrict__ sweeps_out,
+    k_gesvj_warp(int m, int n, T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
+                 T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
+                 int64_t sV0, T tol, int max_sweeps, int *__restrict__ info, int *__restrict__ sweeps_out,
                  int batch) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t mat = (int64_t)blockIdx.x * 4 + warp;
     if (mat >= batch) return;  // the whole warp leaves; no block barriers in this kernel
     const int N = n + (n & 1);
     const bool col = lane < n;
-    float a[MR], v[32];
-    const float *ag = A + mat * sA;
+    T a[MR], v[32];
+    const T *ag = A + mat * sA;
 #pragma unroll
     for (int i = 0; i < MR; i++) a[i] = (col && i < m) ? ag[(int64_t)lane * m + i] : 0.f;
     if (V0) {
         // warm start: V = V0, A <- A V0 (column j of A V0 = sum_k a_k V0(k, j))
-        const float *v0 = V0 + mat * sV0;
+        const T *v0 = V0 + mat * sV0;
 #pragma unroll
         for (int i = 0; i < 32; i++) v[i] = (col && i < n) ? v0[(int64_t)lane * n + i] : 0.f;
-        float b[MR];
+        T b[MR];
 #pragma unroll
         for (int i = 0; i < MR; i++) b[i] = 0.f;
         for (int k = 0; k < n; k++) {
-            float vk = 0.f;  // V0(k, lane)
+            T vk = 0.f;  // V0(k, lane)
 #pragma unroll
             for (int i = 0; i < 32; i++)
                 if (i == k) vk = v[i];
 #pragma unroll
-            for (int i = 0; i < MR; i++) b[i] = fmaf(shfl(a[i], k), vk, b[i]);
+            for (int i = 0; i < MR; i++) b[i] = fma(shfl(a[i], k), vk, b[i]);
         }
 #pragma unroll
         for (int i = 0; i < MR; i++) a[i] = col ? b[i] : 0.f;
@@ -100,11 +108,11 @@ __global__ void __launch_bounds__(128, 1)
         for (int i = 0; i < 32; i++) v[i] = (col && i == lane) ? 1.f : 0.f;
     }
 
-    float fro2 = 0.f;
+    T fro2 = 0.f;
 #pragma unroll
-    for (int i = 0; i < MR; i++) fro2 = fmaf(a[i], a[i], fro2);
-    const float small = FLT_EPSILON * FLT_EPSILON * warp_sum(fro2);
-    tol = jacobi_tol(tol, m);
+    for (int i = 0; i < MR; i++) fro2 = fma(a[i], a[i], fro2);
+    const T small = mach_eps<T>() * mach_eps<T>() * warp_sum(fro2);
+    tol = jacobi_tol<T>(tol, m);
 
     int sweep = 0, converged = 0;
     for (sweep = 1; sweep <= max_sweeps; sweep++) {
@@ -112,30 +120,30 @@ __global__ void __launch_bounds__(128, 1)
         for (int r = 0; r < N - 1; r++) {
             const int partner = rr_partner(lane, r, N);
             const bool active = col && partner < n && partner != lane;
-            float alpha = 0.f, gamma = 0.f;
-            float o[MR];
+            T alpha = 0.f, gamma = 0.f;
+            T o[MR];
 #pragma unroll
             for (int i = 0; i < MR; i++) {
                 o[i] = shfl(a[i], partner);
-                alpha = fmaf(a[i], a[i], alpha);
+                alpha = fma(a[i], a[i], alpha);
             }
-            const float beta_o = shfl(alpha, partner);
+            const T beta_o = shfl(alpha, partner);
             const bool low = lane < partner;  // this lane holds column p of the pair
 #pragma unroll
-            for (int i = 0; i < MR; i++) gamma = fmaf(low ? a[i] : o[i], low ? o[i] : a[i], gamma);
-            float c = 1.f, s = 0.f;
-            const float ap = low ? alpha : beta_o, aq = low ? beta_o : alpha;
-            bool rot = active && jacobi_rotation(ap, aq, gamma, tol, small, c, s);
+            for (int i = 0; i < MR; i++) gamma = fma(low ? a[i] : o[i], low ? o[i] : a[i], gamma);
+            T c = 1.f, s = 0.f;
+            const T ap = low ? alpha : beta_o, aq = low ? beta_o : alpha;
+            bool rot = active && jacobi_rotation<T>(ap, aq, gamma, tol, small, c, s);
             // a_p' = c a_p - s a_q ; a_q' = s a_p + c a_q
-            const float cm = c, so = low ? -s : s;
-            float ov[32];
+            const T cm = c, so = low ? -s : s;
+            T ov[32];
 #pragma unroll
             for (int i = 0; i < 32; i++) ov[i] = shfl(v[i], partner);
             if (rot) {
 #pragma unroll
-                for (int i = 0; i < MR; i++) a[i] = fmaf(cm, a[i], so * o[i]);
+                for (int i = 0; i < MR; i++) a[i] = fma(cm, a[i], so * o[i]);
 #pragma unroll
-                for (int i = 0; i < 32; i++) v[i] = fmaf(cm, v[i], so * ov[i]);
+                for (int i = 0; i < 32; i++) v[i] = fma(cm, v[i], so * ov[i]);
             }
             rotated |= rot;
         }
@@ -148,52 +156,52 @@ __global__ void __launch_bounds__(128, 1)
     // in the error of v_j, so sigma is recomputed from A and V (row by row).
     // U takes the rotated columns themselves, which are orthogonal to the
     // rotation tolerance (A v_j / sigma_j would amplify v_j's error by 1/sigma_j).
-    float nv2 = 0.f;
+    T nv2 = 0.f;
 #pragma unroll
-    for (int i = 0; i < 32; i++) nv2 = fmaf(v[i], v[i], nv2);
-    const float inv_nv = nv2 > 0.f ? 1.f / sqrtf(nv2) : 0.f;
+    for (int i = 0; i < 32; i++) nv2 = fma(v[i], v[i], nv2);
+    const T inv_nv = nv2 > 0.f ? 1.f / sqrt(nv2) : 0.f;
 #pragma unroll
     for (int i = 0; i < 32; i++) v[i] *= inv_nv;
-    float s2 = 0.f;
+    T s2 = 0.f;
     for (int i = 0; i < m; i++) {
-        float bi = 0.f;
+        T bi = 0.f;
 #pragma unroll
         for (int k = 0; k < 32; k++)
-            if (k < n) bi = fmaf(ag[(int64_t)k * m + i], v[k], bi);  // same address in every lane
-        s2 = fmaf(bi, bi, s2);
+            if (k < n) bi = fma(ag[(int64_t)k * m + i], v[k], bi);  // same address in every lane
+        s2 = fma(bi, bi, s2);
     }
-    float rot2 = 0.f;
+    T rot2 = 0.f;
 #pragma unroll
-    for (int i = 0; i < MR; i++) rot2 = fmaf(a[i], a[i], rot2);
-    const float sigma = col ? sqrtf(s2) : -1.f;
+    for (int i = 0; i < MR; i++) rot2 = fma(a[i], a[i], rot2);
+    const T sigma = col ? sqrt(s2) : -1.f;
     int pos = 0;
-    float smax = 0.f;
+    T smax = 0.f;
     for (int k = 0; k < n; k++) {
-        float sk = shfl(sigma, k);
-        smax = fmaxf(smax, sk);
+        T sk = shfl(sigma, k);
+        smax = fmax(smax, sk);
         pos += (sk > sigma || (sk == sigma && k < lane)) ? 1 : 0;
     }
     int imax = 0;
-    float vmax = -1.f;
+    T vmax = -1.f;
 #pragma unroll
     for (int i = 0; i < 32; i++)
-        if (i < n && fabsf(v[i]) > vmax) { vmax = fabsf(v[i]); imax = i; }
-    float vsel = 0.f;
+        if (i < n && fabs(v[i]) > vmax) { vmax = fabs(v[i]); imax = i; }
+    T vsel = 0.f;
 #pragma unroll
     for (int i = 0; i < 32; i++)
         if (i == imax) vsel = v[i];
-    const float sgn = vsel > 0.f ? -1.f : 1.f;
-    const float thr = smax * (float)(m > n ? m : n) * FLT_EPSILON;
+    const T sgn = vsel > 0.f ? -1.f : 1.f;
+    const T thr = smax * (T)(m > n ? m : n) * mach_eps<T>();
     if (col) {
         S[mat * sS + pos] = sigma;
-        float *vt = Vt + mat * sVt;
+        T *vt = Vt + mat * sVt;
 #pragma unroll
         for (int i = 0; i < 32; i++)
             if (i < n) vt[(int64_t)i * n + pos] = sgn * v[i];
     }
     if (U) {
-        float *u = U + mat * sU;
-        const float inv = (sigma > thr && rot2 > 0.f) ? sgn / sqrtf(rot2) : 0.f;
+        T *u = U + mat * sU;
+        const T inv = (sigma > thr && rot2 > 0.f) ? sgn / sqrt(rot2) : 0.f;
         if (col && sigma > thr) {
 #pragma unroll
             for (int i = 0; i < MR; i++)
@@ -204,21 +212,21 @@ __global__ void __launch_bounds__(128, 1)
         __syncwarp();
         // complete U: positions r..m-1
         int c = r, ncomp = 0;
-        const float accept = 0.5f * rsqrtf((float)m);
+        const T accept = T(0.5) * rsqrt((T)m);
         for (int e = 0; e < m && c < m; e++) {
-            float w0 = lane == e ? 1.f : 0.f, w1 = lane + 32 == e ? 1.f : 0.f;
+            T w0 = lane == e ? 1.f : 0.f, w1 = lane + 32 == e ? 1.f : 0.f;
             for (int pass = 0; pass < 2; pass++) {
                 for (int k = 0; k < c; k++) {
-                    float u0 = lane < m ? u[(int64_t)k * m + lane] : 0.f;
-                    float u1 = lane + 32 < m ? u[(int64_t)k * m + lane + 32] : 0.f;
-                    float d = warp_sum(u0 * w0 + u1 * w1);
-                    w0 = fmaf(-d, u0, w0);
-                    w1 = fmaf(-d, u1, w1);
+                    T u0 = lane < m ? u[(int64_t)k * m + lane] : 0.f;
+                    T u1 = lane + 32 < m ? u[(int64_t)k * m + lane + 32] : 0.f;
+                    T d = warp_sum(u0 * w0 + u1 * w1);
+                    w0 = fma(-d, u0, w0);
+                    w1 = fma(-d, u1, w1);
                 }
             }
-            float nw = sqrtf(warp_sum(w0 * w0 + w1 * w1));
+            T nw = sqrt(warp_sum(w0 * w0 + w1 * w1));
             if (nw > accept) {
-                float sc = ((ncomp & 1) ? -1.f : 1.f) / nw;
+                T sc = ((ncomp & 1) ? -1.f : 1.f) / nw;
                 if (lane < m) u[(int64_t)c * m + lane] = w0 * sc;
                 if (lane + 32 < m) u[(int64_t)c * m + lane + 32] = w1 * sc;
                 __syncwarp();
@@ -239,22 +247,24 @@ __global__ void __launch_bounds__(128, 1)
 constexpr int SVJ_CTA_THREADS = 256;
 constexpr int SVJ_GROUP = 8;
 
+template <typename T>
 __global__ void __launch_bounds__(SVJ_CTA_THREADS)
-    k_gesvj_cta(int m, int n, float *__restrict__ A, int64_t sA, float *__restrict__ S, int64_t sS,
-                float *__restrict__ Vt, int64_t sVt, float *__restrict__ U, int64_t sU, const float *__restrict__ V0,
-                int64_t sV0, float tol, int max_sweeps, int *__restrict__ info, int *__restrict__ sweeps_out,
+    k_gesvj_cta(int m, int n, T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
+                T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
+                int64_t sV0, T tol, int max_sweeps, int *__restrict__ info, int *__restrict__ sweeps_out,
                 int batch) {
-    extern __shared__ __align__(16) float svsm[];
+    extern __shared__ __align__(16) unsigned char svsm_raw[];
+    T *svsm = reinterpret_cast<T *>(svsm_raw);
     const int lda = m | 1, ldv = n | 1;
-    float *a = svsm;                      // n columns x lda
-    float *v = a + (size_t)n * lda;       // n columns x ldv
-    float *sig = v + (size_t)n * ldv;     // n
-    float *rinv = sig + n;                // n: 1 / |rotated column j|
+    T *a = svsm;                      // n columns x lda
+    T *v = a + (size_t)n * lda;       // n columns x ldv
+    T *sig = v + (size_t)n * ldv;     // n
+    T *rinv = sig + n;                // n: 1 / |rotated column j|
     const int tid = threadIdx.x, g = tid / SVJ_GROUP, gl = tid % SVJ_GROUP;
     const int N = n + (n & 1), M = N - 1;
 
     for (int64_t mat = blockIdx.x; mat < batch; mat += gridDim.x) {
-        const float *ag = A + mat * sA;
+        const T *ag = A + mat * sA;
         for (int e = tid; e < m * n; e += SVJ_CTA_THREADS) a[(e / m) * lda + e % m] = ag[e];
         for (int e = tid; e < n * n; e += SVJ_CTA_THREADS) {
             int i = e % n, j = e / n;
@@ -266,14 +276,14 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
             for (int i0 = 0; i0 < m; i0 += SVJ_CTA_THREADS / 4) {
                 // each thread: row i0 + tid % 64, columns j = tid / 64 + 4 t
                 const int i = i0 + tid % (SVJ_CTA_THREADS / 4);
-                float acc[16];
+                T acc[16];
                 for (int t = 0; t < 16; t++) acc[t] = 0.f;
                 if (i < m) {
                     for (int k = 0; k < n; k++) {
-                        float aik = a[k * lda + i];
+                        T aik = a[k * lda + i];
                         for (int t = 0; t < 16; t++) {
                             int j = tid / (SVJ_CTA_THREADS / 4) + 4 * t;
-                            if (j < n) acc[t] = fmaf(aik, v[j * ldv + k], acc[t]);
+                            if (j < n) acc[t] = fma(aik, v[j * ldv + k], acc[t]);
                         }
                     }
                 }
@@ -288,15 +298,15 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
         }
         // |A|_F^2 (rotations preserve it) -> threshold below which a column is zero
         if (tid < 32) {
-            float f = 0.f;
+            T f = 0.f;
             for (int j = 0; j < n; j++)
-                for (int i = tid; i < m; i += 32) f = fmaf(a[j * lda + i], a[j * lda + i], f);
+                for (int i = tid; i < m; i += 32) f = fma(a[j * lda + i], a[j * lda + i], f);
             f = warp_sum(f);
             if (tid == 0) sig[0] = f;
         }
         __syncthreads();
-        const float small = FLT_EPSILON * FLT_EPSILON * sig[0];
-        const float tol_eff = jacobi_tol(tol, m);
+        const T small = mach_eps<T>() * mach_eps<T>() * sig[0];
+        const T tol_eff = jacobi_tol<T>(tol, m);
         __syncthreads();
         int sweep = 0, converged = 0;
         for (sweep = 1; sweep <= max_sweeps; sweep++) {
@@ -310,30 +320,30 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
                     q = x < y ? y : x;
                 }
                 const bool act = q >= 0 && q < n;
-                float alpha = 0.f, beta = 0.f, gamma = 0.f;
+                T alpha = 0.f, beta = 0.f, gamma = 0.f;
                 if (act) {
                     for (int i = gl; i < m; i += SVJ_GROUP) {
-                        float x = a[p * lda + i], y = a[q * lda + i];
-                        alpha = fmaf(x, x, alpha);
-                        beta = fmaf(y, y, beta);
-                        gamma = fmaf(x, y, gamma);
+                        T x = a[p * lda + i], y = a[q * lda + i];
+                        alpha = fma(x, x, alpha);
+                        beta = fma(y, y, beta);
+                        gamma = fma(x, y, gamma);
                     }
                 }
                 alpha = group_sum(alpha, SVJ_GROUP);
                 beta = group_sum(beta, SVJ_GROUP);
                 gamma = group_sum(gamma, SVJ_GROUP);
-                float c, s;
-                if (act && jacobi_rotation(alpha, beta, gamma, tol_eff, small, c, s)) {
+                T c, s;
+                if (act && jacobi_rotation<T>(alpha, beta, gamma, tol_eff, small, c, s)) {
                     rotated = 1;
                     for (int i = gl; i < m; i += SVJ_GROUP) {
-                        float x = a[p * lda + i], y = a[q * lda + i];
-                        a[p * lda + i] = fmaf(c, x, -s * y);
-                        a[q * lda + i] = fmaf(s, x, c * y);
+                        T x = a[p * lda + i], y = a[q * lda + i];
+                        a[p * lda + i] = fma(c, x, -s * y);
+                        a[q * lda + i] = fma(s, x, c * y);
                     }
                     for (int i = gl; i < n; i += SVJ_GROUP) {
-                        float x = v[p * ldv + i], y = v[q * ldv + i];
-                        v[p * ldv + i] = fmaf(c, x, -s * y);
-                        v[q * ldv + i] = fmaf(s, x, c * y);
+                        T x = v[p * ldv + i], y = v[q * ldv + i];
+                        v[p * ldv + i] = fma(c, x, -s * y);
+                        v[q * ldv + i] = fma(s, x, c * y);
                     }
                 }
                 __syncthreads();
@@ -345,77 +355,77 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
         // ---- epilogue: normalise V; sigma_j = |A v_j| from the original A (see
         // the warp kernel); U from the rotated columns, normalised
         for (int j = tid / 32; j < n; j += SVJ_CTA_THREADS / 32) {
-            float s2 = 0.f;
-            for (int i = tid % 32; i < n; i += 32) s2 = fmaf(v[j * ldv + i], v[j * ldv + i], s2);
+            T s2 = 0.f;
+            for (int i = tid % 32; i < n; i += 32) s2 = fma(v[j * ldv + i], v[j * ldv + i], s2);
             s2 = warp_sum(s2);
-            const float inv = s2 > 0.f ? 1.f / sqrtf(s2) : 0.f;
+            const T inv = s2 > 0.f ? 1.f / sqrt(s2) : 0.f;
             for (int i = tid % 32; i < n; i += 32) v[j * ldv + i] *= inv;
         }
         __syncthreads();
         for (int j = tid / 32; j < n; j += SVJ_CTA_THREADS / 32) {
-            float s2 = 0.f;
+            T s2 = 0.f;
             for (int i = tid % 32; i < m; i += 32) {
-                float b = 0.f;
-                for (int k = 0; k < n; k++) b = fmaf(ag[(int64_t)k * m + i], v[j * ldv + k], b);
-                s2 = fmaf(b, b, s2);
+                T b = 0.f;
+                for (int k = 0; k < n; k++) b = fma(ag[(int64_t)k * m + i], v[j * ldv + k], b);
+                s2 = fma(b, b, s2);
             }
             s2 = warp_sum(s2);
-            float r2 = 0.f;
-            for (int i = tid % 32; i < m; i += 32) r2 = fmaf(a[j * lda + i], a[j * lda + i], r2);
+            T r2 = 0.f;
+            for (int i = tid % 32; i < m; i += 32) r2 = fma(a[j * lda + i], a[j * lda + i], r2);
             r2 = warp_sum(r2);
             if (tid % 32 == 0) {
-                sig[j] = sqrtf(s2);
-                rinv[j] = r2 > 0.f ? 1.f / sqrtf(r2) : 0.f;
+                sig[j] = sqrt(s2);
+                rinv[j] = r2 > 0.f ? 1.f / sqrt(r2) : 0.f;
             }
         }
         __syncthreads();
-        float smax = 0.f;
-        for (int k = 0; k < n; k++) smax = fmaxf(smax, sig[k]);
-        const float thr = smax * (float)(m > n ? m : n) * FLT_EPSILON;
+        T smax = 0.f;
+        for (int k = 0; k < n; k++) smax = fmax(smax, sig[k]);
+        const T thr = smax * (T)(m > n ? m : n) * mach_eps<T>();
         for (int j = tid; j < n; j += SVJ_CTA_THREADS) {
             int ps = 0;
             for (int k = 0; k < n; k++) ps += (sig[k] > sig[j] || (sig[k] == sig[j] && k < j)) ? 1 : 0;
-            const float inv_rot = rinv[j];
+            const T inv_rot = rinv[j];
             // sign: largest-magnitude entry of v_j made negative
             int imax = 0;
-            float vmax = -1.f;
+            T vmax = -1.f;
             for (int i = 0; i < n; i++)
-                if (fabsf(v[j * ldv + i]) > vmax) { vmax = fabsf(v[j * ldv + i]); imax = i; }
-            float sg = v[j * ldv + imax] > 0.f ? -1.f : 1.f;
+                if (fabs(v[j * ldv + i]) > vmax) { vmax = fabs(v[j * ldv + i]); imax = i; }
+            T sg = v[j * ldv + imax] > 0.f ? -1.f : 1.f;
             S[mat * sS + ps] = sig[j];
             for (int i = 0; i < n; i++) Vt[mat * sVt + (int64_t)i * n + ps] = sg * v[j * ldv + i];
             if (U && sig[j] > thr) {
-                float inv = sg * inv_rot;
+                T inv = sg * inv_rot;
                 for (int i = 0; i < m; i++) U[mat * sU + (int64_t)ps * m + i] = a[j * lda + i] * inv;
             }
         }
         __syncthreads();
         if (U && tid < 32) {
             // complete U (positions r..m-1) with warp 0, rows lane + 32 t
-            float *u = U + mat * sU;
+            T *u = U + mat * sU;
             int r = 0;
             for (int k = 0; k < n; k++) r += sig[k] > thr ? 1 : 0;
             int c = r, ncomp = 0;
-            const float accept = 0.5f * rsqrtf((float)m);
+            const T accept = T(0.5) * rsqrt((T)m);
             for (int e = 0; e < m && c < m; e++) {
-                float w[4];
+                T w[4];
                 for (int t = 0; t < 4; t++) w[t] = (tid + 32 * t == e) ? 1.f : 0.f;
                 for (int pass = 0; pass < 2; pass++)
                     for (int k = 0; k < c; k++) {
-                        float uk[4], d = 0.f;
+                        T uk[4], d = 0.f;
                         for (int t = 0; t < 4; t++) {
                             int i = tid + 32 * t;
                             uk[t] = i < m ? u[(int64_t)k * m + i] : 0.f;
-                            d = fmaf(uk[t], w[t], d);
+                            d = fma(uk[t], w[t], d);
                         }
                         d = warp_sum(d);
-                        for (int t = 0; t < 4; t++) w[t] = fmaf(-d, uk[t], w[t]);
+                        for (int t = 0; t < 4; t++) w[t] = fma(-d, uk[t], w[t]);
                     }
-                float nw = 0.f;
-                for (int t = 0; t < 4; t++) nw = fmaf(w[t], w[t], nw);
-                nw = sqrtf(warp_sum(nw));
+                T nw = 0.f;
+                for (int t = 0; t < 4; t++) nw = fma(w[t], w[t], nw);
+                nw = sqrt(warp_sum(nw));
                 if (nw > accept) {
-                    float sc = ((ncomp & 1) ? -1.f : 1.f) / nw;
+                    T sc = ((ncomp & 1) ? -1.f : 1.f) / nw;
                     for (int t = 0; t < 4; t++) {
                         int i = tid + 32 * t;
                         if (i < m) u[(int64_t)c * m + i] = w[t] * sc;
@@ -434,8 +444,9 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
     }
 }
 
+template <typename T>
 static size_t svj_cta_smem(int m, int n) {
-    return sizeof(float) * ((size_t)n * (m | 1) + (size_t)n * (n | 1) + 2 * (size_t)n) + 16;
+    return sizeof(T) * ((size_t)n * (m | 1) + (size_t)n * (n | 1) + 2 * (size_t)n) + 16;
 }
 
 // ---------------------------------------------------------------- rank
@@ -489,39 +500,85 @@ __global__ void k_nullspace_finish(int n, int m, const T *__restrict__ Uall, con
     }
 }
 
-static gbla_status svd_launch(int m, int n, float *A, int64_t sA, float *S, int64_t sS, float *Vt, int64_t sVt,
-                              float *U, int64_t sU, const float *V0, int64_t sV0, float tol, int max_sweeps, int *info,
-                              int *sweeps, int batch, cudaStream_t st) {
-    if (m < 0 || n < 0 || batch < 0 || m < n || max_sweeps < 1 || !(tol > 0.f)) return GBLA_INVALID_VALUE;
+template <typename T>
+static gbla_status svd_launch(int m, int n, T *A, int64_t sA, T *S, int64_t sS, T *Vt, int64_t sVt, T *U, int64_t sU,
+                              const T *V0, int64_t sV0, T tol, int max_sweeps, int *info, int *sweeps, int batch,
+                              cudaStream_t st) {
+    if (m < 0 || n < 0 || batch < 0 || m < n || max_sweeps < 1 || !(tol > T(0))) return GBLA_INVALID_VALUE;
     if (batch == 0 || n == 0) return GBLA_SUCCESS;
     if (!A || !S || !Vt || sA < (int64_t)m * n || sS < n || sVt < (int64_t)n * n) return GBLA_INVALID_VALUE;
     if (U && sU < (int64_t)m * m) return GBLA_INVALID_VALUE;
     if (V0 && sV0 < (int64_t)n * n) return GBLA_INVALID_VALUE;
-    if (n <= 32 && m <= 64) {
+    // the warp kernel keeps a column of A (MR rows) and of V in registers
+    const int warp_m = sizeof(T) == 4 ? 64 : 32;
+    if (n <= 32 && m <= warp_m) {
         const unsigned grid = (unsigned)((batch + 3) / 4);
-        if (m <= 32)
-            k_gesvj_warp<32><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, info,
-                                                   sweeps, batch);
-        else
-            k_gesvj_warp<64><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, info,
-                                                   sweeps, batch);
+        if (m <= 32) {
+            k_gesvj_warp<T, 32><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps,
+                                                      info, sweeps, batch);
+        } else if constexpr (sizeof(T) == 4) {
+            k_gesvj_warp<T, 64><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps,
+                                                      info, sweeps, batch);
+        }
         return launch_status();
     }
     if (n <= 64 && m <= 128) {
-        size_t smem = svj_cta_smem(m, n);
+        size_t smem = svj_cta_smem<T>(m, n);
         if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k_gesvj_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaError_t e = cudaFuncSetAttribute(k_gesvj_cta<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return from_cuda(e);
         }
         int per_sm = (int)((200 * 1024) / (smem + 1024));
         per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
         int64_t grid = (int64_t)sm_count() * per_sm;
         if (grid > batch) grid = batch;
-        k_gesvj_cta<<<(unsigned)grid, SVJ_CTA_THREADS, smem, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol,
-                                                                 max_sweeps, info, sweeps, batch);
+        k_gesvj_cta<T><<<(unsigned)grid, SVJ_CTA_THREADS, smem, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol,
+                                                                    max_sweeps, info, sweeps, batch);
         return launch_status();
     }
     return GBLA_NOT_SUPPORTED;
+}
+
+template <typename T>
+static gbla_status rank_launch(int len, const T *S, int64_t sS, T eps, unsigned *rank, int batch, cudaStream_t st) {
+    if (len < 0 || batch < 0 || sS < len) return GBLA_INVALID_VALUE;
+    if (batch == 0) return GBLA_SUCCESS;
+    if (!rank || (len > 0 && !S)) return GBLA_INVALID_VALUE;
+    k_rank<T><<<(unsigned)((batch * 32 + 255) / 256), 256, 0, st>>>(len, S, sS, eps, rank, batch);
+    return launch_status();
+}
+
+// workspace layout for the null space: A^T (n x m), S (m), Vt (m x m), U (n x n) per matrix
+static int64_t ns_elems(int m, int n) { return (int64_t)n * m + m + (int64_t)m * m + (int64_t)n * n; }
+
+template <typename T>
+static size_t ns_bytes(int m, int n, int batch) {
+    if (m < 0 || n < 0 || batch < 0) return 0;
+    return (size_t)(ns_elems(m, n) * batch) * sizeof(T) + 256;
+}
+
+template <typename T>
+static gbla_status nullspace_launch(int m, int n, const T *A, int64_t sA, T *N, T *P, unsigned *nullity, T eps,
+                                    int *info, void *workspace, size_t ws_bytes, int batch, cudaStream_t st) {
+    if (m < 1 || n < 0 || m > n || batch < 0) return GBLA_INVALID_VALUE;
+    if (batch == 0 || n == 0) return GBLA_SUCCESS;
+    if (!A || !N || !P || !workspace || sA < (int64_t)m * n) return GBLA_INVALID_VALUE;
+    if (ws_bytes < ns_bytes<T>(m, n, batch)) return GBLA_WORKSPACE_TOO_SMALL;
+    T *At = static_cast<T *>(workspace);
+    T *S = At + (int64_t)n * m * batch;
+    T *Vt = S + (int64_t)m * batch;
+    T *U = Vt + (int64_t)m * m * batch;
+    gbla_status s;
+    if constexpr (sizeof(T) == 4) s = gbla_stranspose_batched(m, n, A, sA, At, (int64_t)n * m, batch, st);
+    else s = gbla_dtranspose_batched(m, n, A, sA, At, (int64_t)n * m, batch, st);
+    if (s != GBLA_SUCCESS) return s;
+    // SVD of A^T (n x m, tall) with the full U (n x n), at working-precision tolerance
+    s = svd_launch<T>(n, m, At, (int64_t)n * m, S, m, Vt, (int64_t)m * m, U, (int64_t)n * n, nullptr, 0,
+                      sizeof(T) == 4 ? T(1e-7) : T(1e-15), 80, info, nullptr, batch, st);
+    if (s != GBLA_SUCCESS) return s;
+    int grid = batch < sm_count() * 4 ? batch : sm_count() * 4;
+    k_nullspace_finish<T><<<grid, 256, 0, st>>>(n, m, U, S, eps, N, P, nullity, batch);
+    return launch_status();
 }
 
 }  // namespace gbla
@@ -531,44 +588,30 @@ using namespace gbla;
 GBLA_API gbla_status gbla_sgesvj_batched(int m, int n, float *A, int64_t sA, float *S, int64_t sS, float *Vt,
                                          int64_t sVt, float *U, int64_t sU, const float *V0, int64_t sV0, float tol,
                                          int max_sweeps, int *info, int *sweeps, int batch, cudaStream_t st) {
-    return svd_launch(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, info, sweeps, batch, st);
+    return svd_launch<float>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, info, sweeps, batch, st);
 }
-
+GBLA_API gbla_status gbla_dgesvj_batched(int m, int n, double *A, int64_t sA, double *S, int64_t sS, double *Vt,
+                                         int64_t sVt, double *U, int64_t sU, const double *V0, int64_t sV0, double tol,
+                                         int max_sweeps, int *info, int *sweeps, int batch, cudaStream_t st) {
+    return svd_launch<double>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, info, sweeps, batch, st);
+}
 GBLA_API gbla_status gbla_srank_batched(int len, const float *S, int64_t sS, float eps, unsigned *rank, int batch,
                                         cudaStream_t st) {
-    if (len < 0 || batch < 0 || sS < len) return GBLA_INVALID_VALUE;
-    if (batch == 0) return GBLA_SUCCESS;
-    if (!rank || (len > 0 && !S)) return GBLA_INVALID_VALUE;
-    k_rank<float><<<(unsigned)((batch * 32 + 255) / 256), 256, 0, st>>>(len, S, sS, eps, rank, batch);
-    return launch_status();
+    return rank_launch<float>(len, S, sS, eps, rank, batch, st);
 }
-
-// workspace layout for gbla_snullspace_batched: A^T (n x m), S (m), Vt (m x m), U (n x n) per matrix
-static int64_t ns_elems(int m, int n) { return (int64_t)n * m + m + (int64_t)m * m + (int64_t)n * n; }
-
-GBLA_API size_t gbla_snullspace_workspace_bytes(int m, int n, int batch) {
-    if (m < 0 || n < 0 || batch < 0) return 0;
-    return (size_t)(ns_elems(m, n) * batch) * sizeof(float) + 256;
+GBLA_API gbla_status gbla_drank_batched(int len, const double *S, int64_t sS, double eps, unsigned *rank, int batch,
+                                        cudaStream_t st) {
+    return rank_launch<double>(len, S, sS, eps, rank, batch, st);
 }
-
+GBLA_API size_t gbla_snullspace_workspace_bytes(int m, int n, int batch) { return ns_bytes<float>(m, n, batch); }
+GBLA_API size_t gbla_dnullspace_workspace_bytes(int m, int n, int batch) { return ns_bytes<double>(m, n, batch); }
 GBLA_API gbla_status gbla_snullspace_batched(int m, int n, const float *A, int64_t sA, float *N, float *P,
                                              unsigned *nullity, float eps, int *info, void *workspace,
                                              size_t ws_bytes, int batch, cudaStream_t st) {
-    if (m < 1 || n < 0 || m > n || batch < 0) return GBLA_INVALID_VALUE;
-    if (batch == 0 || n == 0) return GBLA_SUCCESS;
-    if (!A || !N || !P || !workspace || sA < (int64_t)m * n) return GBLA_INVALID_VALUE;
-    if (ws_bytes < gbla_snullspace_workspace_bytes(m, n, batch)) return GBLA_WORKSPACE_TOO_SMALL;
-    float *At = static_cast<float *>(workspace);
-    float *S = At + (int64_t)n * m * batch;
-    float *Vt = S + (int64_t)m * batch;
-    float *U = Vt + (int64_t)m * m * batch;
-    gbla_status s = gbla_stranspose_batched(m, n, A, sA, At, (int64_t)n * m, batch, st);
-    if (s != GBLA_SUCCESS) return s;
-    // SVD of A^T (n x m, tall) with the full U (n x n); tolerance at FP32 level
-    s = svd_launch(n, m, At, (int64_t)n * m, S, m, Vt, (int64_t)m * m, U, (int64_t)n * n, nullptr, 0, 1e-7f, 60,
-                   info, nullptr, batch, st);
-    if (s != GBLA_SUCCESS) return s;
-    int grid = batch < sm_count() * 4 ? batch : sm_count() * 4;
-    k_nullspace_finish<float><<<grid, 256, 0, st>>>(n, m, U, S, eps, N, P, nullity, batch);
-    return launch_status();
+    return nullspace_launch<float>(m, n, A, sA, N, P, nullity, eps, info, workspace, ws_bytes, batch, st);
+}
+GBLA_API gbla_status gbla_dnullspace_batched(int m, int n, const double *A, int64_t sA, double *N, double *P,
+                                             unsigned *nullity, double eps, int *info, void *workspace,
+                                             size_t ws_bytes, int batch, cudaStream_t st) {
+    return nullspace_launch<double>(m, n, A, sA, N, P, nullity, eps, info, workspace, ws_bytes, batch, st);
 }

@@ -172,13 +172,14 @@ gbla_status gbla_dgels_batched(int m, int n, int nrhs, double *A, int64_t stride
 
 /* ------------------------------------------------------------------- SVD */
 /* One-sided (Hestenes) Jacobi SVD A_i = U_i diag(S_i) Vt_i of m x n matrices
- * (m >= n; n <= 32 with m <= 64, or n <= 64 with m <= 128), all in FP32.
+ * (m >= n; n <= 64, m <= 128), in the precision of the data (s: FP32,
+ * d: FP64; tol' below uses the unit roundoff of that precision).
  * S_i: n singular values, descending.  Vt_i: n x n (= V^T, as Svd::
  * rightSingularVectors returns).  U_i: m x m, nullable (computeU = false).
  * A_i is destroyed (it ends as A_i V_i).  V0 (nullable): n x n orthogonal warm
  * start; A_i V0_i is orthogonalised and V starts at V0.  A pair of columns is
- * rotated while |a_p.a_q| > tol' |a_p||a_q|, tol' = max(tol, 4 sqrt(m) 2^-24)
- * (FP32 columns cannot be more orthogonal than that); singular values are
+ * rotated while |a_p.a_q| > tol' |a_p||a_q|, tol' = max(tol, 4 sqrt(m) u)
+ * (stored columns cannot be more orthogonal than that); singular values are
  * recomputed as |A v_j| at the end.  info[i] = 1 if max_sweeps sweeps
  * did not converge (nullable), sweeps[i] = sweeps used (nullable).  Sign
  * rule: the largest-magnitude entry of each v_j is negative.
@@ -188,12 +189,18 @@ gbla_status gbla_sgesvj_batched(int m, int n, float *A, int64_t strideA, float *
                                 int64_t strideVt, float *U, int64_t strideU, const float *V0, int64_t strideV0,
                                 float tol, int max_sweeps, int *info, int *sweeps, int batch,
                                 cudaStream_t stream);
+gbla_status gbla_dgesvj_batched(int m, int n, double *A, int64_t strideA, double *S, int64_t strideS, double *Vt,
+                                int64_t strideVt, double *U, int64_t strideU, const double *V0, int64_t strideV0,
+                                double tol, int max_sweeps, int *info, int *sweeps, int batch,
+                                cudaStream_t stream);
 
 /* rank[i] = number of entries of S_i (length len) greater than eps.  Unlike
  * Svd::rank (include/tensor.cuh:1600-1609, kernel :1484-1491) the count is
  * written, not accumulated, so repeated calls agree. */
 gbla_status gbla_srank_batched(int len, const float *S, int64_t strideS, float eps, unsigned int *rank, int batch,
                                cudaStream_t stream);
+gbla_status gbla_drank_batched(int len, const double *S, int64_t strideS, double eps, unsigned int *rank,
+                               int batch, cudaStream_t stream);
 
 /* Null space of square or fat m x n matrices (1 <= m <= n <= 64): N_i (n x n)
  * holds an orthonormal basis of ker(A_i) in its first nullity_i columns
@@ -203,8 +210,12 @@ gbla_status gbla_srank_batched(int len, const float *S, int64_t strideS, float e
  * Replaces the Nullspace constructor (include/tensor.cuh:2044-2079: tr, Svd of
  * A^T with U, rank, and per-matrix copies and gemms). */
 size_t gbla_snullspace_workspace_bytes(int m, int n, int batch);
+size_t gbla_dnullspace_workspace_bytes(int m, int n, int batch);
 gbla_status gbla_snullspace_batched(int m, int n, const float *A, int64_t strideA, float *N, float *P,
                                     unsigned int *nullity, float eps, int *info, void *workspace,
+                                    size_t workspace_bytes, int batch, cudaStream_t stream);
+gbla_status gbla_dnullspace_batched(int m, int n, const double *A, int64_t strideA, double *N, double *P,
+                                    unsigned int *nullity, double eps, int *info, void *workspace,
                                     size_t workspace_bytes, int batch, cudaStream_t stream);
 
 /* ------------------------------------------------------- level-1 / copy */
@@ -271,6 +282,27 @@ gbla_status gbla_scopy_rows(int m, int n, int row_from, int nrows, const float *
                             cudaStream_t stream);
 gbla_status gbla_dcopy_rows(int m, int n, int row_from, int nrows, const double *A, double *out,
                             cudaStream_t stream);
+
+/* -------------------------------------------------------------- Givens */
+/* x_i <- c x_i + s y_i, y_i <- c y_i - s x_i for i < len (strides incx, incy).
+ * Replaces cublas<t>rot in DTensor::applyRightGivensRotation /
+ * applyLeftGivensRotation (include/tensor.cuh:1074-1104).  The _dev forms
+ * read c and s from device memory (GivensAnnihilator, tensor.cuh:2296-2311). */
+gbla_status gbla_srot(int64_t len, float *x, int64_t incx, float *y, int64_t incy, float c, float s,
+                      cudaStream_t stream);
+gbla_status gbla_drot(int64_t len, double *x, int64_t incx, double *y, int64_t incy, double c, double s,
+                      cudaStream_t stream);
+gbla_status gbla_srot_dev(int64_t len, float *x, int64_t incx, float *y, int64_t incy, const float *c,
+                          const float *s, cudaStream_t stream);
+gbla_status gbla_drot_dev(int64_t len, double *x, int64_t incx, double *y, int64_t incy, const double *c,
+                          const double *s, cudaStream_t stream);
+/* out[0..2] = (1/hypot(A(i,j), A(k,j)), A(i,j) out[0], A(k,j) out[0]) for the
+ * column-major matrix A with leading dimension ld: the rotation of rows i and
+ * k that zeroes A(k,j).  Replaces k_givensAnnihilateRHypot
+ * (include/tensor.cuh:2270-2281). */
+gbla_status gbla_sgivens_coeffs(const float *A, int64_t ld, int i, int k, int j, float *out, cudaStream_t stream);
+gbla_status gbla_dgivens_coeffs(const double *A, int64_t ld, int i, int k, int j, double *out,
+                                cudaStream_t stream);
 
 /* -------------------------------------------------------- diagnostics */
 /* Measured FMA throughput of the device (precision 32 or 64), in GFLOP/s,

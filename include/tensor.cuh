@@ -1,0 +1,1076 @@
+/*
+ * tensor.cuh -- drop-in replacement for GPUtils' include/tensor.cuh on GB300.
+ *
+ * Same classes, method names, argument meanings and error behaviour as the
+ * reference header (DTensor<T>, Session, IStatus, Svd, CholeskyFactoriser,
+ * QRFactoriser, Nullspace, CholeskyBatchFactoriser, GivensAnnihilator).  All
+ * numerics go through the C ABI of libgbla.so (gbla.h): link with -lgbla
+ * -lcudart instead of -lcublas -lcusolver.  The header contains no device
+ * code, so it compiles with nvcc or a plain C++17/20 compiler.
+ *
+ * Deliberate differences from the reference (each one a fix or an extension):
+ *  - Svd uses a one-sided Jacobi SVD: singular vectors follow the documented
+ *    sign rule (largest-magnitude entry of each v_j negative) instead of
+ *    whatever gesvd returns; null-space columns of U are a different (equally
+ *    valid) orthonormal basis except in the pinned small cases.
+ *  - Svd::rank writes the count instead of accumulating into it.
+ *  - addAB checks dimensions and handles an output that aliases an input
+ *    (Nullspace::project multiplies in place).
+ *  - leastSquaresBatched and the Cholesky/QR solves accept several
+ *    right-hand-side columns (the reference throws or solves only one).
+ *  - leastSquaresBatched (float) adds one refinement step with an extended-
+ *    precision residual, so x is accurate to FP32 rounding even when the
+ *    residual is large (cuBLAS gelsBatched: about kappa^2 u).
+ *  - operator= releases what the target owned before aliasing the source.
+ *  - Givens bounds are checked on every index, as the reference documents.
+ */
+#ifndef TENSOR_CUH
+#define TENSOR_CUH
+
+#include <algorithm>
+#include <cassert>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <iterator>
+#include <limits>
+#include <memory>
+#include <optional>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "gbla.h"
+
+/* ------------------------------------------------------------- defaults */
+#define DEFAULT_FPX double
+#define THREADS_PER_BLOCK 512
+#if (__cplusplus >= 201703L)
+#define TEMPLATE_WITH_TYPE_T template <typename T = DEFAULT_FPX>
+#else
+#define TEMPLATE_WITH_TYPE_T template <typename T>
+#endif
+#if (__cplusplus >= 202002L)
+#include <concepts>
+#define TEMPLATE_CONSTRAINT_REQUIRES_FPX requires std::floating_point<T>
+#else
+#define TEMPLATE_CONSTRAINT_REQUIRES_FPX
+#endif
+
+inline std::mt19937_64 &gputilsRandomEngine() {
+    static std::mt19937_64 engine{std::random_device{}()};
+    return engine;
+}
+
+TEMPLATE_WITH_TYPE_T
+std::vector<T> generateRealRandomVector(size_t n, T low, T hi) {
+    std::uniform_real_distribution<T> dist(low, hi);
+    std::vector<T> vec(n);
+    for (auto &x : vec) x = dist(gputilsRandomEngine());
+    return vec;
+}
+
+inline std::vector<int> generateIntRandomVector(size_t n, int low, int hi) {
+    std::uniform_int_distribution<int> dist(low, hi);
+    std::vector<int> vec(n);
+    for (auto &x : vec) x = dist(gputilsRandomEngine());
+    return vec;
+}
+
+constexpr size_t numBlocks(size_t n, size_t threads_per_block = THREADS_PER_BLOCK) {
+    return (n / threads_per_block + (n % threads_per_block != 0));
+}
+
+/* ----------------------------------------------------------- error check */
+#define gpuErrChk(status) \
+    { gpuAssert((status), __FILE__, __LINE__); }
+
+inline void gpuAssert(cudaError_t code, const char *file, int line, bool abort = true) {
+    if (code != cudaSuccess) {
+        std::cerr << "cuda error. String: " << cudaGetErrorString(code) << ", file: " << file << ", line: " << line
+                  << "\n";
+        if (abort) exit(code);
+    }
+}
+
+inline void gpuAssert(gbla_status code, const char *file, int line, bool abort = true) {
+    if (code != GBLA_SUCCESS) {
+        std::cerr << "gbla error. Name: " << gbla_status_string(code) << ", file: " << file << ", line: " << line
+                  << "\n";
+        if (abort) exit((int)code);
+    }
+}
+
+namespace gputils_detail {
+// A library call that rejects a size this build does not implement becomes
+// std::invalid_argument (the reference's exception for unusable shapes);
+// every other failure is a library error: print and exit, as gpuErrChk does.
+inline void check(gbla_status s, const char *what) {
+    if (s == GBLA_SUCCESS) return;
+    if (s == GBLA_NOT_SUPPORTED || s == GBLA_INVALID_VALUE)
+        throw std::invalid_argument(std::string("[") + what + "] " + gbla_status_string(s));
+    gpuAssert(s, __FILE__, __LINE__);
+}
+}  // namespace gputils_detail
+
+/* ---------------------------------------------------------------- Session */
+static size_t s_numStreams = 1;
+
+class Session {
+public:
+    static void setStreams(size_t numStreams) { s_numStreams = numStreams; }
+
+    static Session &getInstance() {
+        static Session instance(s_numStreams);
+        return instance;
+    }
+
+private:
+    explicit Session(size_t numStreams) : m_numStreams(numStreams) {
+        m_streams.resize(numStreams);
+        m_reduceWorkspace.resize(numStreams, nullptr);
+        m_scalar.resize(numStreams, nullptr);
+        for (size_t i = 0; i < numStreams; i++) gpuErrChk(cudaStreamCreate(&m_streams[i]));
+    }
+
+    ~Session() {
+        for (size_t i = 0; i < m_numStreams; i++) {
+            if (m_reduceWorkspace[i]) cudaFree(m_reduceWorkspace[i]);
+            if (m_scalar[i]) cudaFree(m_scalar[i]);
+        }
+    }
+
+    std::vector<cudaStream_t> m_streams;
+    std::vector<void *> m_reduceWorkspace;
+    std::vector<double *> m_scalar;
+    size_t m_bytesAllocated = 0;
+    size_t m_numStreams = 1;
+
+public:
+    Session(Session const &) = delete;
+    void operator=(Session const &) = delete;
+
+    /** CUDA stream with index idx (the reference's cuBLAS/cuSOLVER handles are gone). */
+    cudaStream_t stream(size_t idx = 0) const {
+        if (idx >= m_numStreams) throw std::runtime_error("stream index out of range");
+        return m_streams[idx];
+    }
+
+    /** Scratch for the reductions of stream idx (lazily allocated, not counted). */
+    void *reductionWorkspace(size_t idx = 0) {
+        if (!m_reduceWorkspace[idx]) gpuErrChk(cudaMalloc(&m_reduceWorkspace[idx], gbla_reduce_workspace_bytes()));
+        return m_reduceWorkspace[idx];
+    }
+
+    /** One device scalar per stream for reduction results. */
+    double *scalar(size_t idx = 0) {
+        if (!m_scalar[idx]) gpuErrChk(cudaMalloc((void **)&m_scalar[idx], sizeof(double)));
+        return m_scalar[idx];
+    }
+
+    cudaError_t cudaAllocate(void **d, size_t s) {
+        cudaError_t err = cudaMalloc(d, s);
+        if (err == cudaSuccess) m_bytesAllocated += s;
+        return err;
+    }
+
+    size_t totalAllocatedBytes() const { return m_bytesAllocated; }
+
+    void incrementAllocatedBytes(int s) { m_bytesAllocated += s; }
+
+    void synchronizeStream(size_t idx = 0) const {
+        if (idx >= m_numStreams) throw std::runtime_error("stream index out of range");
+        gpuErrChk(cudaStreamSynchronize(m_streams[idx]));
+    }
+
+    void synchronizeAllStreams() const {
+        for (size_t i = 0; i < m_numStreams; i++) synchronizeStream(i);
+    }
+};
+
+/* ------------------------------------------------------ typed ABI dispatch */
+namespace gputils_detail {
+template <typename T> struct is_fp : std::integral_constant<bool, std::is_same_v<T, float> || std::is_same_v<T, double>> {};
+
+#define GBLA_DISPATCH(T, sname, dname, ...) \
+    (std::is_same_v<T, float> ? sname(__VA_ARGS__) : dname(__VA_ARGS__))
+
+inline gbla_status gemm(int m, int n, int k, float a, const float *A, int64_t sA, const float *B, int64_t sB, float b,
+                        float *C, int64_t sC, int batch, cudaStream_t st) {
+    return gbla_sgemm_batched(m, n, k, a, A, sA, B, sB, b, C, sC, batch, GBLA_GEMM_AUTO, st);
+}
+inline gbla_status gemm(int m, int n, int k, double a, const double *A, int64_t sA, const double *B, int64_t sB,
+                        double b, double *C, int64_t sC, int batch, cudaStream_t st) {
+    return gbla_dgemm_batched(m, n, k, a, A, sA, B, sB, b, C, sC, batch, st);
+}
+inline gbla_status transpose(int m, int n, const float *A, float *At, int batch, cudaStream_t st) {
+    return gbla_stranspose_batched(m, n, A, (int64_t)m * n, At, (int64_t)m * n, batch, st);
+}
+inline gbla_status transpose(int m, int n, const double *A, double *At, int batch, cudaStream_t st) {
+    return gbla_dtranspose_batched(m, n, A, (int64_t)m * n, At, (int64_t)m * n, batch, st);
+}
+inline gbla_status axpy(int64_t n, float a, const float *x, float *y, cudaStream_t st) { return gbla_saxpy(n, a, x, y, st); }
+inline gbla_status axpy(int64_t n, double a, const double *x, double *y, cudaStream_t st) { return gbla_daxpy(n, a, x, y, st); }
+inline gbla_status scal(int64_t n, float a, float *x, cudaStream_t st) { return gbla_sscal(n, a, x, st); }
+inline gbla_status scal(int64_t n, double a, double *x, cudaStream_t st) { return gbla_dscal(n, a, x, st); }
+inline gbla_status copy_rows(int m, int n, int r0, int nr, const float *A, float *o, cudaStream_t st) {
+    return gbla_scopy_rows(m, n, r0, nr, A, o, st);
+}
+inline gbla_status copy_rows(int m, int n, int r0, int nr, const double *A, double *o, cudaStream_t st) {
+    return gbla_dcopy_rows(m, n, r0, nr, A, o, st);
+}
+inline gbla_status rot(int64_t n, float *x, int64_t ix, float *y, int64_t iy, float c, float s, cudaStream_t st) {
+    return gbla_srot(n, x, ix, y, iy, c, s, st);
+}
+inline gbla_status rot(int64_t n, double *x, int64_t ix, double *y, int64_t iy, double c, double s, cudaStream_t st) {
+    return gbla_drot(n, x, ix, y, iy, c, s, st);
+}
+inline gbla_status rot_dev(int64_t n, float *x, int64_t ix, float *y, int64_t iy, const float *c, const float *s,
+                           cudaStream_t st) {
+    return gbla_srot_dev(n, x, ix, y, iy, c, s, st);
+}
+inline gbla_status rot_dev(int64_t n, double *x, int64_t ix, double *y, int64_t iy, const double *c, const double *s,
+                           cudaStream_t st) {
+    return gbla_drot_dev(n, x, ix, y, iy, c, s, st);
+}
+inline gbla_status givens(const float *A, int64_t ld, int i, int k, int j, float *o, cudaStream_t st) {
+    return gbla_sgivens_coeffs(A, ld, i, k, j, o, st);
+}
+inline gbla_status givens(const double *A, int64_t ld, int i, int k, int j, double *o, cudaStream_t st) {
+    return gbla_dgivens_coeffs(A, ld, i, k, j, o, st);
+}
+inline gbla_status potrf(int n, float *A, int *info, int batch, cudaStream_t st) {
+    return gbla_spotrf_batched(n, A, (int64_t)n * n, info, batch, st);
+}
+inline gbla_status potrf(int n, double *A, int *info, int batch, cudaStream_t st) {
+    return gbla_dpotrf_batched(n, A, (int64_t)n * n, info, batch, st);
+}
+inline gbla_status potrs(int n, int nrhs, const float *L, float *B, int batch, cudaStream_t st) {
+    return gbla_spotrs_batched(n, nrhs, L, (int64_t)n * n, B, (int64_t)n * nrhs, batch, st);
+}
+inline gbla_status potrs(int n, int nrhs, const double *L, double *B, int batch, cudaStream_t st) {
+    return gbla_dpotrs_batched(n, nrhs, L, (int64_t)n * n, B, (int64_t)n * nrhs, batch, st);
+}
+inline gbla_status gels(int m, int n, int nrhs, float *A, float *B, int batch, cudaStream_t st) {
+    return gbla_sgels_batched(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, 1, batch, st);
+}
+inline gbla_status gels(int m, int n, int nrhs, double *A, double *B, int batch, cudaStream_t st) {
+    return gbla_dgels_batched(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, batch, st);
+}
+inline gbla_status geqrf(int m, int n, float *A, float *tau, int *info, cudaStream_t st) {
+    return gbla_sgeqrf_batched(m, n, A, (int64_t)m * n, tau, n, info, 1, st);
+}
+inline gbla_status geqrf(int m, int n, double *A, double *tau, int *info, cudaStream_t st) {
+    return gbla_dgeqrf_batched(m, n, A, (int64_t)m * n, tau, n, info, 1, st);
+}
+inline gbla_status ormqr(int trans, int m, int nc, int k, const float *A, const float *tau, float *Cm, cudaStream_t st) {
+    return gbla_sormqr_batched(trans, m, nc, k, A, (int64_t)m * k, tau, k, Cm, (int64_t)m * nc, 1, st);
+}
+inline gbla_status ormqr(int trans, int m, int nc, int k, const double *A, const double *tau, double *Cm,
+                         cudaStream_t st) {
+    return gbla_dormqr_batched(trans, m, nc, k, A, (int64_t)m * k, tau, k, Cm, (int64_t)m * nc, 1, st);
+}
+inline gbla_status trsm_upper(int n, int nc, const float *R, int64_t ldr, float *B, int64_t ldb, cudaStream_t st) {
+    return gbla_strsm_upper_batched(n, nc, R, ldr, ldr * n, B, ldb, ldb * nc, 1, st);
+}
+inline gbla_status trsm_upper(int n, int nc, const double *R, int64_t ldr, double *B, int64_t ldb, cudaStream_t st) {
+    return gbla_dtrsm_upper_batched(n, nc, R, ldr, ldr * n, B, ldb, ldb * nc, 1, st);
+}
+inline gbla_status gesvj(int m, int n, float *A, float *S, float *Vt, float *U, int *info, int batch, cudaStream_t st) {
+    return gbla_sgesvj_batched(m, n, A, (int64_t)m * n, S, n, Vt, (int64_t)n * n, U, (int64_t)m * m, nullptr, 0, 1e-6f,
+                               60, info, nullptr, batch, st);
+}
+inline gbla_status gesvj(int m, int n, double *A, double *S, double *Vt, double *U, int *info, int batch,
+                         cudaStream_t st) {
+    return gbla_dgesvj_batched(m, n, A, (int64_t)m * n, S, n, Vt, (int64_t)n * n, U, (int64_t)m * m, nullptr, 0, 1e-14,
+                               80, info, nullptr, batch, st);
+}
+inline gbla_status rank(int len, const float *S, float eps, unsigned *r, int batch, cudaStream_t st) {
+    return gbla_srank_batched(len, S, len, eps, r, batch, st);
+}
+inline gbla_status rank(int len, const double *S, double eps, unsigned *r, int batch, cudaStream_t st) {
+    return gbla_drank_batched(len, S, len, eps, r, batch, st);
+}
+inline size_t nullspace_ws(float *, int m, int n, int batch) { return gbla_snullspace_workspace_bytes(m, n, batch); }
+inline size_t nullspace_ws(double *, int m, int n, int batch) { return gbla_dnullspace_workspace_bytes(m, n, batch); }
+inline gbla_status nullspace(int m, int n, const float *A, float *N, float *P, float eps, void *ws, size_t wsb,
+                             int batch, cudaStream_t st) {
+    return gbla_snullspace_batched(m, n, A, (int64_t)m * n, N, P, nullptr, eps, nullptr, ws, wsb, batch, st);
+}
+inline gbla_status nullspace(int m, int n, const double *A, double *N, double *P, double eps, void *ws, size_t wsb,
+                             int batch, cudaStream_t st) {
+    return gbla_dnullspace_batched(m, n, A, (int64_t)m * n, N, P, nullptr, eps, nullptr, ws, wsb, batch, st);
+}
+// whole-buffer reductions; the scalar is read back synchronously (the
+// reference's cuBLAS calls return host scalars)
+enum class Red { Dot, Nrm2, Asum, Amax, Amin };
+template <typename T>
+inline T reduce(Red op, int64_t n, const T *x, const T *y, size_t streamIdx) {
+    Session &s = Session::getInstance();
+    T *res = reinterpret_cast<T *>(s.scalar(streamIdx));
+    void *ws = s.reductionWorkspace(streamIdx);
+    cudaStream_t st = s.stream(streamIdx);
+    gbla_status r = GBLA_SUCCESS;
+    if constexpr (std::is_same_v<T, float>) {
+        switch (op) {
+            case Red::Dot: r = gbla_sdot(n, x, y, res, ws, st); break;
+            case Red::Nrm2: r = gbla_snrm2(n, x, res, ws, st); break;
+            case Red::Asum: r = gbla_sasum(n, x, res, ws, st); break;
+            case Red::Amax: r = gbla_samax(n, x, res, ws, st); break;
+            case Red::Amin: r = gbla_samin(n, x, res, ws, st); break;
+        }
+    } else {
+        switch (op) {
+            case Red::Dot: r = gbla_ddot(n, x, y, res, ws, st); break;
+            case Red::Nrm2: r = gbla_dnrm2(n, x, res, ws, st); break;
+            case Red::Asum: r = gbla_dasum(n, x, res, ws, st); break;
+            case Red::Amax: r = gbla_damax(n, x, res, ws, st); break;
+            case Red::Amin: r = gbla_damin(n, x, res, ws, st); break;
+        }
+    }
+    check(r, "reduction");
+    T host{};
+    gpuErrChk(cudaMemcpyAsync(&host, res, sizeof(T), cudaMemcpyDeviceToHost, st));
+    gpuErrChk(cudaStreamSynchronize(st));
+    return host;
+}
+}  // namespace gputils_detail
+
+/* ---------------------------------------------------------------- DTensor */
+enum StorageMode {
+    columnMajor,
+    rowMajor,
+    defaultMajor = columnMajor
+};
+
+TEMPLATE_WITH_TYPE_T
+class DTensor {
+private:
+    T *m_d_data = nullptr;
+    T **m_d_ptrMatrices = nullptr;
+    size_t m_numRows = 0;
+    size_t m_numCols = 0;
+    size_t m_numMats = 0;
+    bool m_doDestroyData = false;
+    bool m_doDestroyPtrMatrices = false;
+    size_t m_idxStream = 0;
+
+    void destroy() {
+        if (m_doDestroyData) {
+            if (m_d_data) gpuErrChk(cudaFree(m_d_data));
+            m_d_data = nullptr;
+            Session::getInstance().incrementAllocatedBytes(-(int)(m_numRows * m_numCols * m_numMats * sizeof(T)));
+            m_doDestroyData = false;
+        }
+        if (m_doDestroyPtrMatrices) {
+            if (m_d_ptrMatrices) gpuErrChk(cudaFree(m_d_ptrMatrices));
+            m_d_ptrMatrices = nullptr;
+            Session::getInstance().incrementAllocatedBytes(-(int)(m_numMats * sizeof(T *)));
+            m_doDestroyPtrMatrices = false;
+        }
+    }
+
+    void allocateOnDevice(size_t size, bool zero = false) {
+        if (size == 0) return;
+        size_t r = m_numRows, c = m_numCols, k = m_numMats;
+        destroy();
+        m_numRows = r; m_numCols = c; m_numMats = k;
+        m_doDestroyData = true;
+        size_t buffer_size = size * sizeof(T);
+        gpuErrChk(Session::getInstance().cudaAllocate((void **)&m_d_data, buffer_size));
+        if (zero) gpuErrChk(cudaMemset(m_d_data, 0, buffer_size));
+        if (numMats() > 1) {
+            m_doDestroyPtrMatrices = true;
+            cudaError_t st = Session::getInstance().cudaAllocate((void **)&m_d_ptrMatrices, numMats() * sizeof(T *));
+            if (st != cudaSuccess) {
+                gpuErrChk(cudaFree(m_d_data));
+                gpuErrChk(st);
+            }
+        } else {
+            m_doDestroyPtrMatrices = false;
+        }
+    }
+
+    void rm2cm(const std::vector<T> &rm, std::vector<T> &cm) {
+        size_t n = m_numRows * m_numCols;
+        for (size_t k = 0; k < m_numMats; k++) {
+            size_t idx = k * n;
+            for (size_t r = 0; r < m_numRows; r++)
+                for (size_t c = 0; c < m_numCols; c++) cm[idx + (r + c * m_numRows)] = rm[idx + (c + r * m_numCols)];
+        }
+    }
+
+    std::ostream &print(std::ostream &out) const {
+        size_t nr = m_numRows, nc = m_numCols, nm = m_numMats;
+        out << "Tensor [" << m_numRows << " x " << m_numCols << " x " << m_numMats << "]:" << std::endl;
+        std::vector<T> temp;
+        download(temp);
+        for (size_t k = 0; k < nm; k++) {
+            out << ">> layer: " << k << std::endl;
+            for (size_t i = 0; i < nr; i++) {
+                for (size_t j = 0; j < nc; j++) out << std::setw(10) << temp[nr * (nc * k + j) + i] << ", ";
+                out << std::endl;
+            }
+        }
+        return out;
+    }
+
+    // the pointer array exists for API compatibility (ptrMatrices()); the
+    // library itself uses base pointer + stride
+    void initialisePointersToMatricesData() {
+        if (m_numMats <= 1 || !m_d_ptrMatrices || !m_doDestroyPtrMatrices) return;
+        std::vector<T *> h(m_numMats);
+        size_t numelMat = m_numRows * m_numCols;
+        for (size_t i = 0; i < m_numMats; i++) h[i] = m_d_data + i * numelMat;
+        gpuErrChk(cudaMemcpy(m_d_ptrMatrices, h.data(), m_numMats * sizeof(T *), cudaMemcpyHostToDevice));
+    }
+
+    cudaStream_t st() const { return Session::getInstance().stream(m_idxStream); }
+
+    template <typename U> friend class DTensor;
+
+public:
+    DTensor<T> setStreamIdx(size_t idx) {
+        if (idx >= s_numStreams) throw std::invalid_argument("Invalid stream index; it exceeds the max allocated streams");
+        m_idxStream = idx;
+        return *this;
+    }
+
+    size_t streamIdx() const { return m_idxStream; }
+
+    static DTensor<T> createRandomTensor(size_t numRows, size_t numCols, size_t numMats, T low, T hi) {
+        if constexpr (std::is_floating_point<T>::value) {
+            auto v = generateRealRandomVector<T>(numRows * numCols * numMats, low, hi);
+            return DTensor<T>(v, numRows, numCols, numMats);
+        } else if constexpr (std::is_same_v<T, int>) {
+            auto v = generateIntRandomVector(numRows * numCols * numMats, low, hi);
+            return DTensor<T>(v, numRows, numCols, numMats);
+        }
+        throw std::invalid_argument("[createRandomTensor] unsupported type T");
+    }
+
+    static DTensor<T> parseFromFile(std::string path_to_file, StorageMode mode = StorageMode::defaultMajor);
+
+    DTensor() = default;
+
+    ~DTensor() { destroy(); }
+
+    DTensor(size_t m, size_t n = 1, size_t k = 1, bool zero = false) {
+        m_numRows = m; m_numCols = n; m_numMats = k;
+        allocateOnDevice(m * n * k, zero);
+        initialisePointersToMatricesData();
+    }
+
+    DTensor(const std::vector<T> &data, size_t m, size_t n = 1, size_t k = 1,
+            StorageMode mode = StorageMode::defaultMajor) {
+        m_numRows = m; m_numCols = n; m_numMats = k;
+        allocateOnDevice(m * n * k);
+        upload(data, mode);
+        initialisePointersToMatricesData();
+    }
+
+    DTensor(const DTensor &other) {
+        m_numMats = other.m_numMats; m_numRows = other.m_numRows; m_numCols = other.m_numCols;
+        m_idxStream = other.m_idxStream;
+        allocateOnDevice(m_numRows * m_numCols * m_numMats);
+        if (numEl())
+            gpuErrChk(cudaMemcpy(m_d_data, other.raw(), numEl() * sizeof(T), cudaMemcpyDeviceToDevice));
+        initialisePointersToMatricesData();
+    }
+
+    DTensor(DTensor &&other) {
+        m_numCols = other.m_numCols; m_numRows = other.m_numRows; m_numMats = other.m_numMats;
+        m_d_data = other.m_d_data;
+        m_doDestroyData = other.m_doDestroyData;
+        m_doDestroyPtrMatrices = other.m_doDestroyPtrMatrices;
+        m_d_ptrMatrices = other.m_d_ptrMatrices;
+        m_idxStream = other.m_idxStream;
+        other.m_doDestroyPtrMatrices = false;
+        other.m_doDestroyData = false;
+        other.m_d_ptrMatrices = nullptr;
+        other.m_d_data = nullptr;
+        other.m_numCols = other.m_numRows = other.m_numMats = 0;
+    }
+
+    DTensor(const DTensor &other, size_t axis, size_t from, size_t to) {
+        if (from > to) throw std::invalid_argument("from > to");
+        size_t offset = 0, len = to - from + 1;
+        m_d_ptrMatrices = nullptr;
+        if (axis == 2) {
+            offset = other.m_numRows * other.m_numCols * from;
+            m_numRows = other.m_numRows; m_numCols = other.m_numCols; m_numMats = len;
+            m_d_ptrMatrices = other.m_d_ptrMatrices ? other.m_d_ptrMatrices + from : nullptr;
+        } else if (axis == 1) {
+            offset = other.m_numRows * from;
+            m_numRows = other.m_numRows; m_numCols = len; m_numMats = 1;
+        } else if (axis == 0) {
+            offset = from;
+            m_numRows = len; m_numCols = 1; m_numMats = 1;
+        }
+        m_d_data = other.m_d_data + offset;
+        m_doDestroyData = false;
+        m_doDestroyPtrMatrices = false;
+        m_idxStream = other.m_idxStream;
+    }
+
+    T *raw() const { return m_d_data; }
+    T **ptrMatrices() const { return m_d_ptrMatrices; }
+    size_t numRows() const { return m_numRows; }
+    size_t numCols() const { return m_numCols; }
+    size_t numMats() const { return m_numMats; }
+    size_t numEl() const { return m_numRows * m_numCols * m_numMats; }
+
+    bool upload(const std::vector<T> &vec, StorageMode mode = StorageMode::defaultMajor) {
+        size_t size = vec.size(), thisSize = numEl();
+        if (size != thisSize) throw std::invalid_argument("[upload] vec has wrong size");
+        std::vector<T> vecCm(thisSize);
+        if (mode == StorageMode::rowMajor) rm2cm(vec, vecCm);
+        else vecCm = vec;
+        if (thisSize) gpuErrChk(cudaMemcpy(m_d_data, vecCm.data(), size * sizeof(T), cudaMemcpyHostToDevice));
+        return true;
+    }
+
+    void download(std::vector<T> &vec) const {
+        vec.resize(numEl());
+        if (numEl()) gpuErrChk(cudaMemcpy(vec.data(), m_d_data, numEl() * sizeof(T), cudaMemcpyDeviceToHost));
+    }
+
+    void deviceCopyTo(DTensor<T> &elsewhere) const {
+        if (elsewhere.numEl() < numEl()) throw std::invalid_argument("[deviceCopyTo] tensor does not fit into destination");
+        if (numEl())
+            gpuErrChk(cudaMemcpy(elsewhere.raw(), m_d_data, numEl() * sizeof(T), cudaMemcpyDeviceToDevice));
+    }
+
+    DTensor<T> getRows(size_t rowsFrom, size_t rowsTo, size_t matIdx) const {
+        if (rowsFrom > rowsTo || rowsTo >= m_numRows || matIdx >= m_numMats)
+            throw std::invalid_argument("[getRows] rows or matrix out of range");
+        size_t len = rowsTo - rowsFrom + 1;
+        DTensor<T> rowsOnly(len, numCols(), 1);
+        gputils_detail::check(gputils_detail::copy_rows((int)m_numRows, (int)m_numCols, (int)rowsFrom, (int)len,
+                                                        raw() + matIdx * m_numRows * m_numCols, rowsOnly.raw(), st()),
+                              "getRows");
+        return rowsOnly;
+    }
+
+    DTensor<T> tr() const {
+        DTensor<T> transposes(m_numCols, m_numRows, m_numMats);
+        gputils_detail::check(gputils_detail::transpose((int)m_numRows, (int)m_numCols, raw(), transposes.raw(),
+                                                        (int)m_numMats, st()),
+                              "tr");
+        return transposes;
+    }
+
+    T dotF(const DTensor &other) {
+        if (m_numRows != other.m_numRows || m_numCols != other.m_numCols || m_numMats != other.m_numMats)
+            throw std::invalid_argument("[dotF] incompatible dimensions");
+        return gputils_detail::reduce<T>(gputils_detail::Red::Dot, (int64_t)numEl(), raw(), other.raw(), m_idxStream);
+    }
+    T normF() const { return gputils_detail::reduce<T>(gputils_detail::Red::Nrm2, (int64_t)numEl(), raw(), nullptr, m_idxStream); }
+    T sumAbs() const { return gputils_detail::reduce<T>(gputils_detail::Red::Asum, (int64_t)numEl(), raw(), nullptr, m_idxStream); }
+    T maxAbs() const { return gputils_detail::reduce<T>(gputils_detail::Red::Amax, (int64_t)numEl(), raw(), nullptr, m_idxStream); }
+    T minAbs() const { return gputils_detail::reduce<T>(gputils_detail::Red::Amin, (int64_t)numEl(), raw(), nullptr, m_idxStream); }
+
+    /** Right Givens rotation of columns i and j: col_i <- c col_i + s' col_j,
+     *  col_j <- c col_j - s' col_i with s' = *minus_s (host scalars). */
+    void applyRightGivensRotation(size_t i, size_t j, const T *c, const T *minus_s) {
+        if (m_numMats > 1) throw std::invalid_argument("[applyRightGivensRotation] tensors (nMat>1) not supported");
+        if (i >= m_numCols || j >= m_numCols) throw std::invalid_argument("[applyRightGivensRotation] invalid index");
+        gputils_detail::check(gputils_detail::rot((int64_t)m_numRows, m_d_data + i * m_numRows, 1,
+                                                  m_d_data + j * m_numRows, 1, *c, *minus_s, st()),
+                              "applyRightGivensRotation");
+    }
+
+    /** Left Givens rotation of rows i and j (host scalars). */
+    void applyLeftGivensRotation(size_t i, size_t j, const T *c, const T *minus_s) {
+        if (m_numMats > 1) throw std::invalid_argument("[applyLeftGivensRotation] tensors (nMat>1) not supported");
+        if (i >= m_numRows || j >= m_numRows) throw std::invalid_argument("[applyLeftGivensRotation] invalid index");
+        gputils_detail::check(gputils_detail::rot((int64_t)m_numCols, m_d_data + i, (int64_t)m_numRows, m_d_data + j,
+                                                  (int64_t)m_numRows, *c, *minus_s, st()),
+                              "applyLeftGivensRotation");
+    }
+
+    /** Same rotation with c and -s read from device memory. */
+    void applyLeftGivensRotationDevice(size_t i, size_t j, const T *d_c, const T *d_minus_s) {
+        if (i >= m_numRows || j >= m_numRows) throw std::invalid_argument("[applyLeftGivensRotation] invalid index");
+        gputils_detail::check(gputils_detail::rot_dev((int64_t)m_numCols, m_d_data + i, (int64_t)m_numRows,
+                                                      m_d_data + j, (int64_t)m_numRows, d_c, d_minus_s, st()),
+                              "applyLeftGivensRotation");
+    }
+
+    void leastSquaresBatched(DTensor &B) {
+        if (B.numRows() != m_numRows) throw std::invalid_argument("[Least squares batched] rhs rows does not equal lhs rows");
+        if (B.numCols() < 1) throw std::invalid_argument("[Least squares batched] rhs are not vectors");
+        if (B.numMats() != m_numMats) throw std::invalid_argument("[Least squares batched] rhs numMats does not equal lhs numMats");
+        if (m_numCols > m_numRows) throw std::invalid_argument("[Least squares batched] supports square or tall matrices only");
+        gputils_detail::check(gputils_detail::gels((int)m_numRows, (int)m_numCols, (int)B.numCols(), raw(), B.raw(),
+                                                   (int)m_numMats, st()),
+                              "leastSquaresBatched");
+    }
+
+    void addAB(const DTensor<T> &A, const DTensor<T> &B, T alpha = 1, T beta = 0) {
+        size_t nMat = A.numMats(), nRA = A.numRows(), nCA = A.numCols(), nCB = B.numCols();
+        if (B.numRows() != nCA || m_numRows != nRA || m_numCols != nCB || B.numMats() < nMat || m_numMats < nMat)
+            throw std::invalid_argument("[addAB] incompatible dimensions");
+        if (nRA * nCB * nMat == 0) return;
+        // an output that overlaps an input (Nullspace::project: b = P b) goes through a copy
+        auto overlaps = [&](const DTensor<T> &X) {
+            const char *c0 = (const char *)raw(), *c1 = c0 + numEl() * sizeof(T);
+            const char *x0 = (const char *)X.raw(), *x1 = x0 + X.numEl() * sizeof(T);
+            return c0 < x1 && x0 < c1;
+        };
+        std::unique_ptr<DTensor<T>> Acopy, Bcopy;
+        const T *pa = A.raw(), *pb = B.raw();
+        if (overlaps(A)) { Acopy = std::make_unique<DTensor<T>>(A); pa = Acopy->raw(); }
+        if (overlaps(B)) { Bcopy = std::make_unique<DTensor<T>>(B); pb = Bcopy->raw(); }
+        gputils_detail::check(gputils_detail::gemm((int)nRA, (int)nCB, (int)nCA, alpha, pa, (int64_t)(nRA * nCA), pb,
+                                                   (int64_t)(nCA * nCB), beta, raw(), (int64_t)(nRA * nCB),
+                                                   (int)nMat, st()),
+                              "addAB");
+        if (Acopy || Bcopy) gpuErrChk(cudaStreamSynchronize(st()));
+    }
+
+    void reshape(size_t newNumRows, size_t newNumCols, size_t newNumMats = 1) {
+        if (m_numRows == newNumRows && m_numCols == newNumCols && m_numMats == newNumMats) return;
+        size_t newNumElements = newNumRows * newNumCols * newNumMats;
+        if (numEl() != newNumElements) {
+            char msg[256];
+            snprintf(msg, sizeof msg,
+                     "DTensor[%zu x %zu x %zu] with %zu elements cannot be reshaped into DTensor[%zu x %zu x %zu] (%zu elements)",
+                     numRows(), numCols(), numMats(), numEl(), newNumRows, newNumCols, newNumMats, newNumElements);
+            throw std::invalid_argument(msg);
+        }
+        if (newNumMats > m_numMats) {
+            if (m_d_ptrMatrices && m_doDestroyPtrMatrices) {
+                gpuErrChk(cudaFree(m_d_ptrMatrices));
+                Session::getInstance().incrementAllocatedBytes(-(int)(m_numMats * sizeof(T *)));
+                m_d_ptrMatrices = nullptr;
+                m_doDestroyPtrMatrices = false;
+            }
+            if (newNumMats > 1) {
+                gpuErrChk(Session::getInstance().cudaAllocate((void **)&m_d_ptrMatrices, newNumMats * sizeof(T *)));
+                m_doDestroyPtrMatrices = true;
+            }
+        }
+        m_numRows = newNumRows;
+        m_numCols = newNumCols;
+        m_numMats = newNumMats;
+        initialisePointersToMatricesData();
+    }
+
+    void saveToFile(std::string pathToFile);
+
+    /* ------------- OPERATORS ------------- */
+    DTensor &operator=(const DTensor &other) {
+        if (this == &other) return *this;
+        destroy();  // the reference leaks what the target owned
+        m_numMats = other.m_numMats;
+        m_numRows = other.m_numRows;
+        m_numCols = other.m_numCols;
+        m_doDestroyData = false;
+        m_doDestroyPtrMatrices = false;
+        m_d_data = other.m_d_data;
+        m_d_ptrMatrices = other.m_d_ptrMatrices;
+        m_idxStream = other.m_idxStream;
+        return *this;
+    }
+
+    T operator()(size_t i, size_t j = 0, size_t k = 0) const {
+        T hostDst;
+        size_t offset = i + m_numRows * (j + m_numCols * k);
+        gpuErrChk(cudaMemcpy(&hostDst, m_d_data + offset, sizeof(T), cudaMemcpyDeviceToHost));
+        return hostDst;
+    }
+
+    DTensor &operator*=(T scalar) {
+        static_assert(gputils_detail::is_fp<T>::value, "operator*= needs float or double");
+        gputils_detail::check(gputils_detail::scal((int64_t)numEl(), scalar, m_d_data, st()), "operator*=");
+        return *this;
+    }
+
+    DTensor &operator+=(const DTensor &rhs) {
+        static_assert(gputils_detail::is_fp<T>::value, "operator+= needs float or double");
+        gputils_detail::check(gputils_detail::axpy((int64_t)numEl(), T(1), rhs.m_d_data, m_d_data, st()), "operator+=");
+        return *this;
+    }
+
+    DTensor &operator-=(const DTensor &rhs) {
+        static_assert(gputils_detail::is_fp<T>::value, "operator-= needs float or double");
+        gputils_detail::check(gputils_detail::axpy((int64_t)numEl(), T(-1), rhs.m_d_data, m_d_data, st()), "operator-=");
+        return *this;
+    }
+
+    /* ------------- FRIENDS ------------- */
+    friend DTensor operator+(DTensor &first, const DTensor &second) {
+        DTensor result(first);
+        result += second;
+        return result;
+    }
+
+    friend DTensor operator-(DTensor &first, const DTensor &second) {
+        DTensor result(first);
+        result -= second;
+        return result;
+    }
+
+    friend DTensor<T> operator*(DTensor &A, DTensor &B) {
+        DTensor<T> result(A.m_numRows, B.m_numCols, B.m_numMats);
+        result.addAB(A, B);
+        return result;
+    }
+
+    friend DTensor<T> operator*(T a, DTensor &B) {
+        DTensor<T> result(B);
+        result *= a;
+        return result;
+    }
+
+    friend std::ostream &operator<<(std::ostream &out, const DTensor<T> &data) { return data.print(out); }
+};
+
+/* ------------------------------------------------------ file input / output */
+template <typename T>
+struct data_t {
+    size_t numRows;
+    size_t numCols;
+    size_t numMats;
+    std::vector<T> data;
+};
+
+template <typename T>
+data_t<T> vectorFromTextFile(std::string path_to_file) {
+    data_t<T> d;
+    std::ifstream file(path_to_file, std::ios::in);
+    if (!file.is_open()) throw std::invalid_argument("[vectorFromTextFile] the file does not exist");
+    std::string line;
+    getline(file, line); d.numRows = std::stoull(line);
+    getline(file, line); d.numCols = std::stoull(line);
+    getline(file, line); d.numMats = std::stoull(line);
+    size_t numElements = d.numRows * d.numCols * d.numMats;
+    d.data.resize(numElements);
+    size_t i = 0;
+    while (i < numElements && getline(file, line)) {
+        if constexpr (std::is_same_v<T, int>) d.data[i] = std::stoi(line);
+        else if constexpr (std::is_same_v<T, double>) d.data[i] = std::stod(line);
+        else if constexpr (std::is_same_v<T, float>) d.data[i] = std::stof(line);
+        else if constexpr (std::is_same_v<T, long double>) d.data[i] = std::stold(line);
+        else if constexpr (std::is_same_v<T, long>) d.data[i] = std::stol(line);
+        else if constexpr (std::is_same_v<T, long long>) d.data[i] = std::stoll(line);
+        else if constexpr (std::is_same_v<T, unsigned long> || std::is_same_v<T, unsigned long long>)
+            d.data[i] = (T)std::stoull(line);
+        else if constexpr (std::is_same_v<T, unsigned int>) d.data[i] = (T)std::stoul(line);
+        else throw std::invalid_argument("data type not supported");
+        i++;
+    }
+    return d;
+}
+
+template <typename T>
+data_t<T> vectorFromBinaryFile(std::string path_to_file) {
+    data_t<T> d;
+    std::ifstream in(path_to_file, std::ios::binary);
+    if (!in.is_open()) throw std::invalid_argument("[vectorFromBinaryFile] the file does not exist");
+    uint64_t hdr[3] = {0, 0, 0};
+    in.read(reinterpret_cast<char *>(hdr), sizeof hdr);
+    d.numRows = hdr[0]; d.numCols = hdr[1]; d.numMats = hdr[2];
+    d.data.resize(d.numRows * d.numCols * d.numMats);
+    in.read(reinterpret_cast<char *>(d.data.data()), (std::streamsize)(d.data.size() * sizeof(T)));
+    return d;
+}
+
+template <typename T>
+DTensor<T> DTensor<T>::parseFromFile(std::string path_to_file, StorageMode mode) {
+    std::string ext = path_to_file.size() >= 3 ? path_to_file.substr(path_to_file.size() - 3) : "";
+    auto parsed = (ext == ".bt") ? vectorFromBinaryFile<T>(path_to_file) : vectorFromTextFile<T>(path_to_file);
+    return DTensor<T>(parsed.data, parsed.numRows, parsed.numCols, parsed.numMats, mode);
+}
+
+template <typename T>
+void DTensor<T>::saveToFile(std::string pathToFile) {
+    std::vector<T> myData(numEl());
+    download(myData);
+    std::string ext = pathToFile.size() >= 3 ? pathToFile.substr(pathToFile.size() - 3) : "";
+    if (ext == ".bt") {
+        uint64_t hdr[3] = {(uint64_t)numRows(), (uint64_t)numCols(), (uint64_t)numMats()};
+        std::ofstream out(pathToFile, std::ios::binary);
+        out.write(reinterpret_cast<const char *>(hdr), sizeof hdr);
+        out.write(reinterpret_cast<const char *>(myData.data()), (std::streamsize)(myData.size() * sizeof(T)));
+    } else {
+        std::ofstream file(pathToFile);
+        file << numRows() << std::endl << numCols() << std::endl << numMats() << std::endl;
+        if constexpr (std::is_floating_point<T>::value) file << std::setprecision(std::numeric_limits<T>::max_digits10);
+        for (const T &el : myData) file << el << std::endl;
+    }
+}
+
+/* ------------------------------------------------------------------ IStatus */
+class IStatus {
+protected:
+    std::unique_ptr<DTensor<int>> m_info;
+
+    IStatus(size_t n = 1) { m_info = std::make_unique<DTensor<int>>(1, 1, n, true); }
+
+public:
+    virtual ~IStatus() = default;
+    virtual DTensor<int> &info() { return *m_info; }
+};
+
+/* ---------------------------------------------------------------------- Svd */
+TEMPLATE_WITH_TYPE_T
+TEMPLATE_CONSTRAINT_REQUIRES_FPX
+class Svd : public IStatus {
+private:
+    DTensor<T> *m_tensor = nullptr;
+    std::shared_ptr<DTensor<T>> m_Vtr;
+    std::shared_ptr<DTensor<T>> m_S;
+    std::shared_ptr<DTensor<T>> m_U;
+    std::shared_ptr<DTensor<unsigned int>> m_rank;
+    bool m_computeU = false;
+    bool m_destroyMatrix = true;
+
+    void checkMatrix(DTensor<T> &tensor) const {
+        if (tensor.numRows() < tensor.numCols()) throw std::invalid_argument("[svd] your matrix is fat (no offence)");
+    }
+
+public:
+    Svd(DTensor<T> &mat, bool computeU = false, bool destroyMatrix = true) : IStatus(mat.numMats()) {
+        checkMatrix(mat);
+        m_destroyMatrix = destroyMatrix;
+        m_tensor = destroyMatrix ? &mat : new DTensor<T>(mat);
+        m_computeU = computeU;
+        size_t m = mat.numRows(), n = mat.numCols(), k = mat.numMats();
+        m_Vtr = std::make_shared<DTensor<T>>(n, n, k);
+        m_S = std::make_shared<DTensor<T>>(std::min(m, n), 1, k);
+        m_rank = std::make_shared<DTensor<unsigned int>>(1, 1, k, true);
+        if (computeU) m_U = std::make_shared<DTensor<T>>(m, m, k);
+    }
+
+    ~Svd() {
+        if (!m_destroyMatrix && m_tensor) delete m_tensor;
+    }
+
+    /** Batched one-sided Jacobi SVD of every matrix (one launch). */
+    void factorise() {
+        size_t m = m_tensor->numRows(), n = m_tensor->numCols(), k = m_tensor->numMats();
+        cudaStream_t st = Session::getInstance().stream(m_tensor->streamIdx());
+        gputils_detail::check(gputils_detail::gesvj((int)m, (int)n, m_tensor->raw(), m_S->raw(), m_Vtr->raw(),
+                                                    m_computeU ? m_U->raw() : nullptr, m_info->raw(), (int)k, st),
+                              "svd");
+    }
+
+    DTensor<T> &singularValues() const { return *m_S; }
+    DTensor<T> const &rightSingularVectors() const { return *m_Vtr; }
+
+    std::optional<std::shared_ptr<DTensor<T>>> leftSingularVectors() const {
+        if (!m_computeU) return std::nullopt;
+        return m_U;
+    }
+
+    /** Number of singular values greater than epsilon, per matrix (written,
+     *  not accumulated). */
+    DTensor<unsigned int> const &rank(T epsilon = 1e-6) const {
+        cudaStream_t st = Session::getInstance().stream(m_tensor->streamIdx());
+        gputils_detail::check(gputils_detail::rank((int)(m_S->numRows() * m_S->numCols()), m_S->raw(), epsilon,
+                                                   m_rank->raw(), (int)m_rank->numMats(), st),
+                              "rank");
+        return *m_rank;
+    }
+};
+
+/* ------------------------------------------------------- CholeskyFactoriser */
+TEMPLATE_WITH_TYPE_T
+TEMPLATE_CONSTRAINT_REQUIRES_FPX
+class CholeskyFactoriser : public IStatus {
+private:
+    DTensor<T> *m_matrix;
+
+public:
+    CholeskyFactoriser(DTensor<T> &A) : IStatus() {
+        if (A.numMats() > 1) throw std::invalid_argument("[Cholesky] 3D tensors require `CholeskyBatchFactoriser`");
+        if (A.numRows() != A.numCols()) throw std::invalid_argument("[Cholesky] Matrix A must be square");
+        m_matrix = &A;
+    }
+
+    void factorise() {
+        gputils_detail::check(gputils_detail::potrf((int)m_matrix->numRows(), m_matrix->raw(), m_info->raw(), 1,
+                                                    Session::getInstance().stream(m_matrix->streamIdx())),
+                              "Cholesky");
+    }
+
+    void solve(DTensor<T> &b) {
+        size_t n = m_matrix->numRows();
+        if (b.numRows() != n) throw std::invalid_argument("[Cholesky] A and b incompatible");
+        gputils_detail::check(gputils_detail::potrs((int)n, (int)(b.numCols() * b.numMats()), m_matrix->raw(), b.raw(),
+                                                    1, Session::getInstance().stream(m_matrix->streamIdx())),
+                              "Cholesky solve");
+    }
+};
+
+/* ------------------------------------------------------------- QRFactoriser */
+TEMPLATE_WITH_TYPE_T
+TEMPLATE_CONSTRAINT_REQUIRES_FPX
+class QRFactoriser : public IStatus {
+private:
+    std::unique_ptr<DTensor<T>> m_householder;
+    DTensor<T> *m_matrix;
+
+    cudaStream_t st() const { return Session::getInstance().stream(m_matrix->streamIdx()); }
+
+public:
+    QRFactoriser(DTensor<T> &A) : IStatus() {
+        if (A.numMats() > 1) throw std::invalid_argument("[QR] 3D tensors require `leastSquaresBatched`");
+        if (A.numRows() < A.numCols()) throw std::invalid_argument("[QR] Matrix A must be tall or square");
+        m_matrix = &A;
+        m_householder = std::make_unique<DTensor<T>>(m_matrix->numCols());
+    }
+
+    void factorise() {
+        gputils_detail::check(gputils_detail::geqrf((int)m_matrix->numRows(), (int)m_matrix->numCols(),
+                                                    m_matrix->raw(), m_householder->raw(), m_info->raw(), st()),
+                              "QR");
+    }
+
+    /** Solves A x = b in the least-squares sense; x overwrites rows [0, n) of b. */
+    void leastSquares(DTensor<T> &rhs) {
+        int m = (int)m_matrix->numRows(), n = (int)m_matrix->numCols();
+        if ((int)rhs.numRows() != m) throw std::invalid_argument("[QR] A and b incompatible");
+        int nc = (int)(rhs.numCols() * rhs.numMats());
+        gputils_detail::check(gputils_detail::ormqr(1, m, nc, n, m_matrix->raw(), m_householder->raw(), rhs.raw(), st()),
+                              "QR ormqr");
+        gputils_detail::check(gputils_detail::trsm_upper(n, nc, m_matrix->raw(), m, rhs.raw(), m, st()), "QR trsm");
+    }
+
+    /** Explicit Q (m x n) and R (n x n); for debugging. */
+    void getQR(DTensor<T> &Q, DTensor<T> &R) {
+        size_t m = m_matrix->numRows(), n = m_matrix->numCols();
+        if (Q.numRows() != m || Q.numCols() != n) throw std::invalid_argument("[QR] invalid shape of Q.");
+        if (R.numRows() != n || R.numCols() != n) throw std::invalid_argument("[QR] invalid shape of R.");
+        std::vector<T> vecQ(m * n, T(0));
+        for (size_t c = 0; c < n; c++) vecQ[c * m + c] = T(1);
+        Q.upload(vecQ);
+        gputils_detail::check(gputils_detail::ormqr(0, (int)m, (int)n, (int)n, m_matrix->raw(), m_householder->raw(),
+                                                    Q.raw(), st()),
+                              "QR getQR");
+        std::vector<T> a;
+        m_matrix->download(a);
+        std::vector<T> vecR(n * n, T(0));
+        for (size_t c = 0; c < n; c++)
+            for (size_t r = 0; r <= c; r++) vecR[c * n + r] = a[c * m + r];
+        R.upload(vecR);
+    }
+};
+
+/* ---------------------------------------------------------------- Nullspace */
+TEMPLATE_WITH_TYPE_T
+TEMPLATE_CONSTRAINT_REQUIRES_FPX
+class Nullspace {
+private:
+    std::unique_ptr<DTensor<T>> m_nullspace;
+    std::unique_ptr<DTensor<T>> m_projOp;
+
+public:
+    Nullspace(DTensor<T> &a) {
+        size_t m = a.numRows(), n = a.numCols(), k = a.numMats();
+        if (m > n) throw std::invalid_argument("[nullspace] I was expecting a square or fat matrix");
+        m_nullspace = std::make_unique<DTensor<T>>(n, n, k, true);
+        m_projOp = std::make_unique<DTensor<T>>(n, n, k, true);
+        size_t wsb = gputils_detail::nullspace_ws((T *)nullptr, (int)m, (int)n, (int)k);
+        void *ws = nullptr;
+        gpuErrChk(cudaMalloc(&ws, wsb));
+        cudaStream_t st = Session::getInstance().stream(a.streamIdx());
+        gbla_status s = gputils_detail::nullspace((int)m, (int)n, a.raw(), m_nullspace->raw(), m_projOp->raw(),
+                                                  (T)1e-6, ws, wsb, (int)k, st);
+        gpuErrChk(cudaStreamSynchronize(st));
+        cudaFree(ws);
+        gputils_detail::check(s, "nullspace");
+    }
+
+    DTensor<T> const &nullspace() const { return *m_nullspace; }
+
+    /** b_i <- N_i N_i^T b_i for every matrix i. */
+    void project(DTensor<T> &b) { b.addAB(*m_projOp, b, 1, 0); }
+};
+
+/* -------------------------------------------------- CholeskyBatchFactoriser */
+TEMPLATE_WITH_TYPE_T
+TEMPLATE_CONSTRAINT_REQUIRES_FPX
+class CholeskyBatchFactoriser : public IStatus {
+private:
+    DTensor<T> *m_matrix;
+    size_t m_numRows = 0;
+    size_t m_numMats = 0;
+    bool m_factorisationDone = false;
+
+public:
+    CholeskyBatchFactoriser() = delete;
+
+    CholeskyBatchFactoriser(DTensor<T> &A, bool factorised = false) : IStatus(A.numMats()), m_factorisationDone(factorised) {
+        if (A.numRows() != A.numCols()) throw std::invalid_argument("[CholeskyBatch] A must be square");
+        m_matrix = &A;
+        m_numRows = A.numRows();
+        m_numMats = A.numMats();
+    }
+
+    void factorise() {
+        if (m_factorisationDone) return;
+        gputils_detail::check(gputils_detail::potrf((int)m_numRows, m_matrix->raw(), m_info->raw(), (int)m_numMats,
+                                                    Session::getInstance().stream(m_matrix->streamIdx())),
+                              "CholeskyBatch");
+        m_factorisationDone = true;
+    }
+
+    void solve(DTensor<T> &b) {
+        if (!m_factorisationDone) throw std::logic_error("[CholeskyBatchSolve] no factor to solve with");
+        if (m_numRows != b.numRows() || m_numMats != b.numMats())
+            throw std::invalid_argument("[CholeskyBatchSolve] A and b incompatible");
+        gputils_detail::check(gputils_detail::potrs((int)m_numRows, (int)b.numCols(), m_matrix->raw(), b.raw(),
+                                                    (int)m_numMats, Session::getInstance().stream(m_matrix->streamIdx())),
+                              "CholeskyBatchSolve");
+    }
+};
+
+/* ------------------------------------------------------- GivensAnnihilator */
+TEMPLATE_WITH_TYPE_T
+TEMPLATE_CONSTRAINT_REQUIRES_FPX
+class GivensAnnihilator {
+private:
+    DTensor<T> *m_matrix = nullptr;
+    std::unique_ptr<DTensor<T>> m_d_rhyp_cos_sin;
+
+    void init() { m_d_rhyp_cos_sin = std::make_unique<DTensor<T>>(3); }
+
+public:
+    GivensAnnihilator() { init(); }
+
+    GivensAnnihilator(DTensor<T> &a) {
+        if (a.numMats() > 1) throw std::invalid_argument("[GivensAnnihilator] tensors (numMats > 1) not supported");
+        m_matrix = &a;
+        init();
+    }
+
+    void setMatrix(DTensor<T> &a) {
+        if (a.numMats() > 1) throw std::invalid_argument("[GivensAnnihilator] tensors (numMats > 1) not supported");
+        m_matrix = &a;
+    }
+
+    /** Left rotation of rows i and k that zeroes element (k, j). */
+    void annihilate(size_t i, size_t k, size_t j) {
+        size_t nR = m_matrix->numRows(), nC = m_matrix->numCols();
+        if (i >= nR || k >= nR) throw std::invalid_argument("[GivensAnnihilator::annihilate] invalid row index");
+        if (j >= nC) throw std::invalid_argument("[GivensAnnihilator::annihilate] invalid column index j");
+        T *aux = m_d_rhyp_cos_sin->raw();
+        cudaStream_t st = Session::getInstance().stream(m_matrix->streamIdx());
+        gputils_detail::check(gputils_detail::givens(m_matrix->raw(), (int64_t)nR, (int)i, (int)k, (int)j, aux, st),
+                              "GivensAnnihilator");
+        m_matrix->applyLeftGivensRotationDevice(i, k, aux + 1, aux + 2);
+    }
+};
+
+#endif  // TENSOR_CUH

@@ -72,6 +72,9 @@ SCALARS = {
     "chol_L21": (1230, 0),
     "chol_L22": (1231, 0),
     "qr_ls_residual": (1529, 0),
+    "givens_a00": (1726, 0),
+    "givens_a03": (1727, 0),
+    "givens_a13": (1728, 0),
     "precision_low": (5, 0),
     "precision_high": (6, 0),
 }

@@ -12,17 +12,19 @@ G = goldens()
 LOW = G["precision_low"]
 
 
-def _svd(lib, A, compute_u=False, V0=None, tol=1e-6, max_sweeps=40):
+def _svd(lib, A, compute_u=False, V0=None, tol=1e-6, max_sweeps=40, dt=np.float32):
     import torch
     k, m, n = A.shape
-    Ad = to_dev(A, np.float32)
-    S = torch.zeros(k * n, dtype=torch.float32, device="cuda")
-    Vt = torch.zeros(k * n * n, dtype=torch.float32, device="cuda")
-    U = torch.zeros(k * m * m, dtype=torch.float32, device="cuda") if compute_u else None
-    V0d = to_dev(V0, np.float32) if V0 is not None else None
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    Ad = to_dev(A, dt)
+    S = torch.zeros(k * n, dtype=tdt, device="cuda")
+    Vt = torch.zeros(k * n * n, dtype=tdt, device="cuda")
+    U = torch.zeros(k * m * m, dtype=tdt, device="cuda") if compute_u else None
+    V0d = to_dev(V0, dt) if V0 is not None else None
     info = torch.full((k,), -1, dtype=torch.int32, device="cuda")
     sw = torch.zeros(k, dtype=torch.int32, device="cuda")
-    st = lib.gbla_sgesvj_batched(m, n, ptr(Ad), m * n, ptr(S), n, ptr(Vt), n * n,
+    fn = lib.gbla_sgesvj_batched if dt == np.float32 else lib.gbla_dgesvj_batched
+    st = fn(m, n, ptr(Ad), m * n, ptr(S), n, ptr(Vt), n * n,
                                  ptr(U) if compute_u else None, m * m, ptr(V0d) if V0d is not None else None, n * n,
                                  tol, max_sweeps, ptr(info), ptr(sw), k, stream())
     assert st == 0
@@ -178,3 +180,29 @@ def test_d5_family_64_converges(gbla_lib, cuda):
     idx = np.arange(0, 1024, 37)
     o = O.gesvj(A[idx])
     assert rel_err(r["S"][idx][:, None, :], o["S"][:, None, :]) < 1e-6
+
+
+@pytest.mark.parametrize("shape", [(3, 2), (8, 3), (32, 32), (20, 17), (64, 64), (100, 40)])
+def test_double_precision_vs_oracle(gbla_lib, cuda, shape):
+    m, n = shape
+    rng = np.random.default_rng(7 * m + n)
+    A = rng.standard_normal((6, m, n))
+    r = _svd(gbla_lib, A, compute_u=True, tol=1e-14, max_sweeps=60, dt=np.float64)
+    o = O.gesvj(A, compute_u=True)
+    assert (r["info"] == 0).all()
+    assert rel_err(r["S"][:, None, :], o["S"][:, None, :]) < 1e-13
+    rec = r["U"][:, :, :n] @ (r["S"][:, :, None] * r["Vt"])
+    assert rel_err(rec, A) < 1e-12
+
+
+def test_double_reference_goldens(gbla_lib, cuda):
+    HIGH = G["precision_high"]
+    B = colmajor(G["svd_b"], 8, 3)
+    r = _svd(gbla_lib, B, compute_u=True, tol=1e-15, dt=np.float64)
+    assert abs(r["S"][0, 0] - G["svd_sigma1"]) < HIGH and abs(r["S"][0, 1] - G["svd_sigma2"]) < HIGH
+    A = colmajor(G["svd_multi_a"], 3, 2, 3)
+    r = _svd(gbla_lib, A, compute_u=True, tol=1e-15, dt=np.float64)
+    vt_flat = np.concatenate([r["Vt"][i].T.ravel() for i in range(3)])
+    np.testing.assert_allclose(vt_flat[:4], G["svd_multi_vt"][:4], atol=HIGH)
+    u_flat = np.concatenate([r["U"][i].T.ravel() for i in range(3)])
+    np.testing.assert_allclose(u_flat, G["svd_multi_u"], atol=HIGH)
