@@ -19,6 +19,7 @@ _CTYPES = {
     "int": C.c_int,
     "unsigned int": C.c_uint,
     "int64_t": C.c_int64,
+    "uint64_t": C.c_uint64,
     "size_t": C.c_size_t,
     "float": C.c_float,
     "double": C.c_double,

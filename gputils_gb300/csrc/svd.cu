@@ -72,10 +72,10 @@ __device__ __forceinline__ T jacobi_tol(T tol, int m) {
 // ----------------------------------------------------------- warp kernel
 template <typename T, int MR>
 __global__ void __launch_bounds__(128, 1)
-    k_gesvj_warp(int m, int n, T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
+    k_gesvj_warp(int m, int n, const T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
                  T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
-                 int64_t sV0, T tol, int max_sweeps, int *__restrict__ info, int *__restrict__ sweeps_out,
-                 int batch) {
+                 int64_t sV0, T tol, int max_sweeps, int warm_budget, int *__restrict__ fallback_out,
+                 int *__restrict__ info, int *__restrict__ sweeps_out, int batch) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t mat = (int64_t)blockIdx.x * 4 + warp;
     if (mat >= batch) return;  // the whole warp leaves; no block barriers in this kernel
@@ -114,8 +114,13 @@ __global__ void __launch_bounds__(128, 1)
     const T small = mach_eps<T>() * mach_eps<T>() * warp_sum(fro2);
     tol = jacobi_tol<T>(tol, m);
 
-    int sweep = 0, converged = 0;
-    for (sweep = 1; sweep <= max_sweeps; sweep++) {
+    // warm start with a sweep budget: past it, restart cold from A (V = I)
+    const bool budgeted = V0 && warm_budget > 0;
+    int sweep = 0, total = 0, converged = 0, restarted = 0;
+    int limit = budgeted ? warm_budget : max_sweeps;
+    for (;;) {
+    for (sweep = 1; sweep <= limit; sweep++) {
+        total++;
         int rotated = 0;
         for (int r = 0; r < N - 1; r++) {
             const int partner = rr_partner(lane, r, N);
@@ -149,7 +154,14 @@ __global__ void __launch_bounds__(128, 1)
         }
         if (!__any_sync(FULL, rotated)) { converged = 1; break; }
     }
-    if (sweep > max_sweeps) sweep = max_sweeps;
+    if (converged || restarted || !budgeted) break;
+#pragma unroll
+    for (int i = 0; i < MR; i++) a[i] = (col && i < m) ? ag[(int64_t)lane * m + i] : 0.f;
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = (col && i == lane) ? 1.f : 0.f;
+    restarted = 1;
+    limit = max_sweeps;
+    }
 
     // ---- epilogue.  The rotated columns' norms drift by ~sqrt(#rotations) ulp;
     // sigma_j = |A v_j| / |v_j| from the original A is accurate to second order
@@ -237,7 +249,8 @@ __global__ void __launch_bounds__(128, 1)
     }
     if (lane == 0) {
         if (info) info[mat] = converged ? 0 : 1;
-        if (sweeps_out) sweeps_out[mat] = sweep;
+        if (sweeps_out) sweeps_out[mat] = total;
+        if (fallback_out) fallback_out[mat] = restarted;
     }
 }
 
@@ -249,10 +262,10 @@ constexpr int SVJ_GROUP = 8;
 
 template <typename T>
 __global__ void __launch_bounds__(SVJ_CTA_THREADS)
-    k_gesvj_cta(int m, int n, T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
+    k_gesvj_cta(int m, int n, const T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
                 T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
-                int64_t sV0, T tol, int max_sweeps, int *__restrict__ info, int *__restrict__ sweeps_out,
-                int batch) {
+                int64_t sV0, T tol, int max_sweeps, int warm_budget, int *__restrict__ fallback_out,
+                int *__restrict__ info, int *__restrict__ sweeps_out, int batch) {
     extern __shared__ __align__(16) unsigned char svsm_raw[];
     T *svsm = reinterpret_cast<T *>(svsm_raw);
     const int lda = m | 1, ldv = n | 1;
@@ -308,8 +321,12 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
         const T small = mach_eps<T>() * mach_eps<T>() * sig[0];
         const T tol_eff = jacobi_tol<T>(tol, m);
         __syncthreads();
-        int sweep = 0, converged = 0;
-        for (sweep = 1; sweep <= max_sweeps; sweep++) {
+        const bool budgeted = V0 && warm_budget > 0;
+        int sweep = 0, total = 0, converged = 0, restarted = 0;
+        int limit = budgeted ? warm_budget : max_sweeps;
+        for (;;) {
+        for (sweep = 1; sweep <= limit; sweep++) {
+            total++;
             int rotated = 0;
             for (int r = 0; r < M; r++) {
                 int p = -1, q = -1;
@@ -351,7 +368,14 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
             // block-wide OR in one barrier: every thread sees the same decision
             if (!__syncthreads_or(rotated)) { converged = 1; break; }
         }
-        if (sweep > max_sweeps) sweep = max_sweeps;
+        if (converged || restarted || !budgeted) break;
+        // warm budget spent: restart cold from A with V = I
+        for (int e = tid; e < m * n; e += SVJ_CTA_THREADS) a[(e / m) * lda + e % m] = ag[e];
+        for (int e = tid; e < n * n; e += SVJ_CTA_THREADS) v[(e / n) * ldv + e % n] = (e % n == e / n) ? 1.f : 0.f;
+        __syncthreads();
+        restarted = 1;
+        limit = max_sweeps;
+        }
         // ---- epilogue: normalise V; sigma_j = |A v_j| from the original A (see
         // the warp kernel); U from the rotated columns, normalised
         for (int j = tid / 32; j < n; j += SVJ_CTA_THREADS / 32) {
@@ -438,7 +462,8 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
         }
         if (tid == 0) {
             if (info) info[mat] = converged ? 0 : 1;
-            if (sweeps_out) sweeps_out[mat] = sweep;
+            if (sweeps_out) sweeps_out[mat] = total;
+            if (fallback_out) fallback_out[mat] = restarted;
         }
         __syncthreads();
     }
@@ -501,9 +526,9 @@ __global__ void k_nullspace_finish(int n, int m, const T *__restrict__ Uall, con
 }
 
 template <typename T>
-static gbla_status svd_launch(int m, int n, T *A, int64_t sA, T *S, int64_t sS, T *Vt, int64_t sVt, T *U, int64_t sU,
-                              const T *V0, int64_t sV0, T tol, int max_sweeps, int *info, int *sweeps, int batch,
-                              cudaStream_t st) {
+static gbla_status svd_launch(int m, int n, const T *A, int64_t sA, T *S, int64_t sS, T *Vt, int64_t sVt, T *U,
+                              int64_t sU, const T *V0, int64_t sV0, T tol, int max_sweeps, int *info, int *sweeps,
+                              int batch, cudaStream_t st, int warm_budget = 0, int *fallback = nullptr) {
     if (m < 0 || n < 0 || batch < 0 || m < n || max_sweeps < 1 || !(tol > T(0))) return GBLA_INVALID_VALUE;
     if (batch == 0 || n == 0) return GBLA_SUCCESS;
     if (!A || !S || !Vt || sA < (int64_t)m * n || sS < n || sVt < (int64_t)n * n) return GBLA_INVALID_VALUE;
@@ -515,10 +540,10 @@ static gbla_status svd_launch(int m, int n, T *A, int64_t sA, T *S, int64_t sS, 
         const unsigned grid = (unsigned)((batch + 3) / 4);
         if (m <= 32) {
             k_gesvj_warp<T, 32><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps,
-                                                      info, sweeps, batch);
+                                                      warm_budget, fallback, info, sweeps, batch);
         } else if constexpr (sizeof(T) == 4) {
             k_gesvj_warp<T, 64><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps,
-                                                      info, sweeps, batch);
+                                                      warm_budget, fallback, info, sweeps, batch);
         }
         return launch_status();
     }
@@ -533,7 +558,8 @@ static gbla_status svd_launch(int m, int n, T *A, int64_t sA, T *S, int64_t sS, 
         int64_t grid = (int64_t)sm_count() * per_sm;
         if (grid > batch) grid = batch;
         k_gesvj_cta<T><<<(unsigned)grid, SVJ_CTA_THREADS, smem, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol,
-                                                                    max_sweeps, info, sweeps, batch);
+                                                                    max_sweeps, warm_budget, fallback, info, sweeps,
+                                                                    batch);
         return launch_status();
     }
     return GBLA_NOT_SUPPORTED;
@@ -594,6 +620,14 @@ GBLA_API gbla_status gbla_dgesvj_batched(int m, int n, double *A, int64_t sA, do
                                          int64_t sVt, double *U, int64_t sU, const double *V0, int64_t sV0, double tol,
                                          int max_sweeps, int *info, int *sweeps, int batch, cudaStream_t st) {
     return svd_launch<double>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, info, sweeps, batch, st);
+}
+GBLA_API gbla_status gbla_sgesvj_warm_batched(int m, int n, const float *A, int64_t sA, float *S, int64_t sS,
+                                              float *Vt, int64_t sVt, float *U, int64_t sU, const float *V0,
+                                              int64_t sV0, int warm_budget, float tol, int max_sweeps, int *info,
+                                              int *sweeps, int *fallback, int batch, cudaStream_t st) {
+    if (batch > 0 && n > 0 && (!V0 || warm_budget < 1)) return GBLA_INVALID_VALUE;
+    return svd_launch<float>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, info, sweeps, batch, st,
+                             warm_budget, fallback);
 }
 GBLA_API gbla_status gbla_srank_batched(int len, const float *S, int64_t sS, float eps, unsigned *rank, int batch,
                                         cudaStream_t st) {

@@ -304,6 +304,94 @@ gbla_status gbla_sgivens_coeffs(const float *A, int64_t ld, int i, int k, int j,
 gbla_status gbla_dgivens_coeffs(const double *A, int64_t ld, int i, int k, int j, double *out,
                                 cudaStream_t stream);
 
+/* ------------------------------------------ BF16 tensor-core GEMM (TN) */
+/* Fused epilogue of gbla_gemm_bf16_tn, applied per element in this order:
+ * t = alpha * acc; t += bias[n] (nullable); t = max(t, 0) if relu;
+ * t = 0 where mask[m][n] <= 0 (nullable; the ReLU derivative of a stored
+ * activation).  t is then written to every non-null output: out_f32 [M][N]
+ * FP32, out_bf16 [M][N] and out_bf16_t [N][M] (transposed) as BF16 bit
+ * patterns.  ld_* are row strides in elements. */
+typedef struct gbla_bf16_epilogue {
+    float alpha;
+    const float *bias;
+    int relu;
+    const uint16_t *mask;
+    int64_t ld_mask;
+    float *out_f32;
+    int64_t ld_f32;
+    uint16_t *out_bf16;
+    int64_t ld_bf16;
+    uint16_t *out_bf16_t;
+    int64_t ld_bf16_t;
+} gbla_bf16_epilogue;
+
+/* C[M x N] = A[M x K] * B[N x K]^T with BF16 operands (row-major, K
+ * contiguous: lda, ldb >= K, multiples of 8; 16-byte aligned bases) and FP32
+ * accumulation in tensor memory (tcgen05, TMA-fed).  Any M, N, K >= 1; tails
+ * are zero-filled.  No reference counterpart: it carries the warm-start
+ * network below. */
+gbla_status gbla_gemm_bf16_tn(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb,
+                              const gbla_bf16_epilogue *epi, cudaStream_t stream);
+
+/* ------------------------------------------- learned Jacobi warm start */
+/* A small network maps an n x n matrix A (n*n inputs, column-major order) to
+ * the P = n(n-1)/2 strictly-upper entries of a skew matrix S (row-major upper
+ * triangle order: (0,1), (0,2), ..., (0,n-1), (1,2), ...), and the warm-start
+ * frame is V0 = Vb * (I - S)^{-1} (I + S) (a Cayley transform about a fixed
+ * base frame Vb).  Layers: n*n -> hidden -> hidden -> P, ReLU after the two
+ * hidden layers; BF16 weights and activations, FP32 accumulation (tcgen05),
+ * FP32 master weights and Adam state.
+ * Training loss per matrix (mean over the batch): || V0 - V Pi D ||_F^2,
+ * where V is the converged Jacobi frame of A and the column permutation Pi
+ * and signs D are chosen greedily (largest |V0^T V| entry first) so that the
+ * loss measures the distance to the nearest exact eigenbasis.
+ * No reference counterpart: the reference always starts Jacobi cold. */
+typedef struct gbla_wsnet gbla_wsnet;
+
+/* n <= 64 with n*n and n(n-1)/2 multiples of 8 ... (n in {16, 32, 48, 64});
+ * hidden a multiple of 64; max_batch >= 1.  Allocates device memory (not a
+ * hot-path call).  Weights: He-uniform for the hidden layers, zero for the
+ * output layer (so the first prediction is V0 = Vb); Vb = identity. */
+gbla_status gbla_wsnet_create(int n, int hidden, int max_batch, uint64_t seed, gbla_wsnet **net);
+gbla_status gbla_wsnet_destroy(gbla_wsnet *net);
+/* Number of FP32 parameters, laid out flat as W1 [hidden][n*n], b1 [hidden],
+ * W2 [hidden][hidden], b2 [hidden], W3 [P][hidden], b3 [P] (row-major). */
+int64_t gbla_wsnet_param_count(const gbla_wsnet *net);
+/* Device copies of the parameters (set also refreshes the BF16 weights and
+ * clears the Adam state) and of the base frame (n x n column-major). */
+gbla_status gbla_wsnet_get_params(const gbla_wsnet *net, float *params, cudaStream_t stream);
+gbla_status gbla_wsnet_set_params(gbla_wsnet *net, const float *params, cudaStream_t stream);
+gbla_status gbla_wsnet_get_base(const gbla_wsnet *net, float *Vb, cudaStream_t stream);
+gbla_status gbla_wsnet_set_base(gbla_wsnet *net, const float *Vb, cudaStream_t stream);
+/* Loss and gradient of a batch without updating: matrices idx[b] (idx
+ * nullable = 0..batch-1) of A (n x n, stride strideA) and their Jacobi
+ * frames V (stride strideV).  grad: param_count floats (device); loss: one
+ * float (device, mean over the batch); assign (nullable): batch x n ints,
+ * the true column matched to each predicted column as sign * (1 + index). */
+gbla_status gbla_wsnet_gradients(gbla_wsnet *net, const float *A, int64_t strideA, const float *V, int64_t strideV,
+                                 const int *idx, int batch, float *grad, float *loss, int *assign,
+                                 cudaStream_t stream);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) at learning rate lr on
+ * the batch; loss (nullable, device) receives the batch loss before the step. */
+gbla_status gbla_wsnet_train_step(gbla_wsnet *net, const float *A, int64_t strideA, const float *V,
+                                  int64_t strideV, const int *idx, int batch, float lr, float *loss,
+                                  cudaStream_t stream);
+/* Warm-start frames V0 (n x n column-major, stride strideV0) for a batch of
+ * at most max_batch matrices. */
+gbla_status gbla_wsnet_predict(gbla_wsnet *net, const float *A, int64_t strideA, float *V0, int64_t strideV0,
+                               int batch, cudaStream_t stream);
+
+/* Warm-started one-sided Jacobi SVD with cold fallback: as gbla_sgesvj_batched
+ * (n <= 64, m <= 128, U nullable) starting from V0, but a matrix that has not
+ * converged after warm_budget sweeps restarts from A with V = I and runs to
+ * convergence (max_sweeps more at most).  sweeps (nullable) counts all sweeps
+ * of the matrix; fallback (nullable) is 1 where the cold restart ran.  A is
+ * not modified. */
+gbla_status gbla_sgesvj_warm_batched(int m, int n, const float *A, int64_t strideA, float *S, int64_t strideS,
+                                     float *Vt, int64_t strideVt, float *U, int64_t strideU, const float *V0,
+                                     int64_t strideV0, int warm_budget, float tol, int max_sweeps, int *info,
+                                     int *sweeps, int *fallback, int batch, cudaStream_t stream);
+
 /* -------------------------------------------------------- diagnostics */
 /* Measured FMA throughput of the device (precision 32 or 64), in GFLOP/s,
  * from a register-resident FMA probe on every SM.  Allocates and
