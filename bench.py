@@ -70,6 +70,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-reference-library", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
     ap.add_argument("--peaks", action="store_true", help="print the measured FFMA / DFMA rates and exit")
+    ap.add_argument("--ws-pairs", type=int, default=200_000, help="d5: (A, V) training pairs of the warm-start net")
+    ap.add_argument("--ws-epochs", type=int, default=20, help="d5: training epochs of the warm-start net")
     return ap.parse_args(argv)
 
 
@@ -164,8 +166,10 @@ class ClockSampler:
 def peaks():
     if os.path.exists(PEAKS_FILE):
         d = json.load(open(PEAKS_FILE))
-        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
-    return {"hbm_gbs": FALLBACK_PEAKS["hbm_gbs"], "source": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d.get("bf16_tflops", FALLBACK_PEAKS["bf16_tflops"]),
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": FALLBACK_PEAKS["hbm_gbs"], "bf16_tflops": FALLBACK_PEAKS["bf16_tflops"],
+            "bf16_tflops_sustained": None, "source": "fallback"}
 
 
 def traffic_for(kernel: str):
@@ -329,11 +333,16 @@ def workload_config(workload, args=None):
                             f"nrhs 1..8, {dt}, one call (plan + CUDA graph), FP32 factor + refinement",
                 "systems": 20000, "dtype": dt, "parallelism": "replicas",
                 "l2": "inputs larger than L2 every step (per-step copies of the arenas)"}
-    n = 32 if workload == "d4" else 64
-    k = 8192 if workload == "d4" else 32768
-    return {"workload": f"one-sided Jacobi SVD (Svd::factorise, S and V^T) of {k} {n}x{n} fp32 matrices of the "
-                        f"parametric family A0 + sum theta_j A_j, tol 1e-6, cold start",
-            "matrices": k, "n": n, "parallelism": "replicas",
+    if workload == "d5":
+        pairs = getattr(args, "ws_pairs", 200_000) if args is not None else 200_000
+        return {"workload": "learned warm start: one-sided Jacobi SVD (S and V^T) of 32768 64x64 fp32 matrices of "
+                            "the parametric family A0 + sum theta_j A_j, tol 1e-6; each step = network "
+                            "(4096->512->512->2016, BF16 tcgen05) + Cayley frame + warm Jacobi with cold fallback",
+                "matrices": 32768, "n": 64, "train_pairs": pairs, "parallelism": "replicas",
+                "l2": "inputs (537 MB) larger than L2"}
+    return {"workload": "one-sided Jacobi SVD (Svd::factorise, S and V^T) of 8192 32x32 fp32 matrices of the "
+                        "parametric family A0 + sum theta_j A_j, tol 1e-6, cold start",
+            "matrices": 8192, "n": 32, "parallelism": "replicas",
             "l2": "per-step copies of the input (the SVD destroys it)"}
 
 
@@ -801,6 +810,158 @@ def run_ours_svd(args, dev, st, L, rank, world, dist):
     }
 
 
+def run_ours_d5(args, dev, st, L, rank, world, dist):
+    """Learned warm start on the 64 x 64 family: train the network on
+    --ws-pairs (A, V) pairs from the cold Jacobi SVD (setup, untimed), then
+    time network + Cayley frame + warm Jacobi with cold fallback on the
+    32768-matrix batch, next to the cold Jacobi on the same batch."""
+    import torch
+    from gputils_gb300 import workloads, warmstart as W
+    from oracle import oracle as O
+
+    n = 64
+    t0 = time.time()
+    net, stats = W.train_family_model(n=n, family_seed=6, pairs=args.ws_pairs, epochs=args.ws_epochs,
+                                      theta_seed=1234 + rank, seed=rank)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    Ah = workloads.d5_svd64()
+    k = Ah.shape[0]
+    A = torch.from_numpy(np.ascontiguousarray(Ah.transpose(0, 2, 1))).to(dev)
+    V0 = torch.empty_like(A)
+    S = torch.empty((k, n), dtype=torch.float32, device=dev)
+    Vt = torch.empty_like(A)
+    info = torch.empty(k, dtype=torch.int32, device=dev)
+    sweeps = torch.empty(k, dtype=torch.int32, device=dev)
+    fb = torch.empty(k, dtype=torch.int32, device=dev)
+    budget = net.warm_budget
+
+    def warm_step(Ad):
+        net.predict(Ad, out=V0)
+        _lib_check(L.gbla_sgesvj_warm_batched(n, n, Ad.data_ptr(), n * n, S.data_ptr(), n, Vt.data_ptr(), n * n,
+                                              None, 0, V0.data_ptr(), n * n, budget, 1e-6, 60, info.data_ptr(),
+                                              sweeps.data_ptr(), fb.data_ptr(), k, st), "gesvj_warm")
+
+    def cold_step(Ad):
+        _lib_check(L.gbla_sgesvj_batched(n, n, Ad.data_ptr(), n * n, S.data_ptr(), n, Vt.data_ptr(), n * n, None,
+                                         0, None, 0, 1e-6, 60, info.data_ptr(), sweeps.data_ptr(), k, st), "gesvj")
+
+    def timed(fn, steps, clocks=False):
+        for _ in range(args.warmup):
+            fn(A)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clk = ClockSampler(torch.cuda.current_device()) if clocks else None
+        if clk:
+            clk.__enter__()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(steps):
+            fn(A)
+        e1.record()
+        torch.cuda.synchronize()
+        if clk:
+            clk.__exit__(None, None, None)
+        return e0.elapsed_time(e1) / 1e3, (clk.summary() if clk else None)
+
+    idx = np.arange(0, k, 512)
+    So = O.gesvj(Ah[idx], tol=1e-12)["S"]
+    # cold, for the comparison
+    cold_t, _ = timed(cold_step, max(2, args.steps // 2))
+    cold_steps = max(2, args.steps // 2)
+    assert (info.cpu().numpy() == 0).all()
+    sw_cold = sweeps.cpu().numpy().copy()
+    err_cold = rel_err(S.cpu().numpy()[idx][:, None, :], So[:, None, :])
+    # warm (the measured path)
+    elapsed, clocks = timed(warm_step, args.steps, clocks=True)
+    elapsed_max, units_all = aggregate(elapsed, k * args.steps, world, dist, dev)
+    assert (info.cpu().numpy() == 0).all()
+    sw = sweeps.cpu().numpy()
+    fbk = fb.cpu().numpy()
+    err = rel_err(S.cpu().numpy()[idx][:, None, :], So[:, None, :])
+    # kernel split of one warm step: network + frame, then Jacobi
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record()
+    net.predict(A, out=V0)
+    e[1].record()
+    _lib_check(L.gbla_sgesvj_warm_batched(n, n, A.data_ptr(), n * n, S.data_ptr(), n, Vt.data_ptr(), n * n, None, 0,
+                                          V0.data_ptr(), n * n, budget, 1e-6, 60, info.data_ptr(), sweeps.data_ptr(),
+                                          fb.data_ptr(), k, st), "gesvj_warm")
+    e[2].record()
+    torch.cuda.synchronize()
+    t_net, t_jac = e[0].elapsed_time(e[1]) / 1e3, e[1].elapsed_time(e[2]) / 1e3
+
+    # end to end: pinned host A in, S and V^T out, every step
+    hA = torch.from_numpy(np.ascontiguousarray(Ah.transpose(0, 2, 1))).pin_memory()
+    hS = torch.empty((k, n), dtype=torch.float32).pin_memory()
+    hVt = torch.empty((k, n, n), dtype=torch.float32).pin_memory()
+    Ad = torch.empty_like(A)
+
+    def e2e_step():
+        Ad.copy_(hA, non_blocking=True)
+        warm_step(Ad)
+        hS.copy_(S, non_blocking=True)
+        hVt.copy_(Vt, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    esteps = max(3, min(args.steps, 5))
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(esteps):
+        e2e_step()
+    f1.record()
+    torch.cuda.synchronize()
+    e2e_t = f0.elapsed_time(f1) / 1e3 / esteps
+    e2e_max, _ = aggregate(e2e_t, 0.0, world, dist, dev)
+
+    reflib = None
+    if not args.no_reference_library:
+        try:
+            reflib = reference_library_svd(dev, st, A, Ah, n, args.ref_sample or 128)
+        except Exception as exc:
+            reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
+    t = elapsed_max / args.steps
+    flops = (4 * n ** 3 + 8 * n ** 3) * k
+    mlp_flops = 2 * (4096 * 512 + 512 * 512 + 512 * 2016) * k
+    pk = peaks()
+    net.close()
+    return {
+        "metric": metric_name(args.workload), "value": units_all / elapsed_max, "unit": "matrices/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network: bf16)",
+        "data": "synthetic (seeded parametric family; training pairs from a separate theta stream)",
+        "config": workload_config(args.workload, args),
+        "roofline": {"bound": "fp32 cuda cores", "achieved": flops / t / 1e12, "peak": FFMA_TFLOPS,
+                     "unit": "TFLOP/s", "frac": flops / t / 1e12 / FFMA_TFLOPS, "traffic": None,
+                     "kernel": "gesvj (warm)", "algorithmic_flops_per_launch": flops,
+                     "peak_source": "measured FFMA rate (gbla_diag_fma_throughput)"},
+        "roofline_network": {"bound": "tensor", "achieved": mlp_flops / t_net / 1e12,
+                             "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                             "frac": mlp_flops / t_net / 1e12 / pk["bf16_tflops"],
+                             "note": "network GEMMs' flops over the whole predict (GEMMs + Cayley frame) time"},
+        "split_ms": {"network_and_frame": t_net * 1e3, "jacobi": t_jac * 1e3},
+        "max_rel_err_vs_fp64": {"sigma": err},
+        "sweeps": {"mean": float(sw.mean()), "max": int(sw.max()), "fallback_fraction": float(fbk.mean()),
+                   "warm_budget": budget},
+        "cold": {"value": k * cold_steps / cold_t, "ms_per_step": cold_t / cold_steps * 1e3,
+                 "sweeps_mean": float(sw_cold.mean()), "sweeps_max": int(sw_cold.max()),
+                 "max_rel_err_vs_fp64": {"sigma": err_cold}},
+        "warm_over_cold": (cold_t / cold_steps) / t,
+        "training": {"pairs": stats["pairs"], "epochs": stats["epochs"], "seconds": train_s,
+                     "loss_first_last": [stats["loss"][0], stats["loss"][-1]],
+                     "cold_sweeps_mean_on_training_pairs": stats["cold_sweeps_mean"]},
+        "gpu_launches": 6 * args.steps, "clocks": clocks, "reference_library": reflib,
+        "e2e": {"value": k / e2e_max, "unit": "matrices/s", "h2d_bytes_per_step": hA.numel() * 4,
+                "d2h_bytes_per_step": (hS.numel() + hVt.numel()) * 4},
+    }
+
+
+def _lib_check(status, what):
+    from gputils_gb300 import _lib
+    _lib.check(status, what)
+
+
 def reference_library_svd(dev, st, A0, Ah, nmat, sample):
     """Svd<float>::factorise: a host loop of cusolverDnSgesvd('N', 'A') over the
     matrices; timed on the first `sample` matrices and scaled (the loop's cost
@@ -947,7 +1108,7 @@ def main(argv=None):
         dist.barrier()
     L = _lib.lib()
     st = torch.cuda.current_stream().cuda_stream
-    runners = {"d1": run_ours_d1, "d2": run_ours_d2, "d3": run_ours_d3, "d4": run_ours_svd, "d5": run_ours_svd}
+    runners = {"d1": run_ours_d1, "d2": run_ours_d2, "d3": run_ours_d3, "d4": run_ours_svd, "d5": run_ours_d5}
     line = runners[args.workload](args, dev, st, L, rank, world, dist)
     cpu = None if args.no_cpu_baseline or rank != 0 else CPU_BASELINES[args.workload](args.cpu_seconds, args)
     line["cpu_baseline"] = cpu

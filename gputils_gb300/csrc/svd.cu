@@ -69,6 +69,46 @@ __device__ __forceinline__ T jacobi_tol(T tol, int m) {
     return tol > floor_ ? tol : floor_;
 }
 
+// Rotation for the block kernel, with the column norms alpha, beta supplied
+// (cached) and t = tan(theta) returned for the norm update.  FP32: the
+// threshold test and the angle (zeta, t) use approximate reciprocals and
+// square roots -- any t gives an exactly orthogonal (c, s) pair -- and c comes
+// from a Newton-refined reciprocal square root, whose remaining bias
+// (-1.5 e^2, e ~ 2^-22) is far below the rounding of the update itself.
+template <typename T>
+__device__ __forceinline__ bool jacobi_rotation_t(T alpha, T beta, T gamma, T tol, T small, T &c, T &s, T &t);
+
+template <>
+__device__ __forceinline__ bool jacobi_rotation_t<float>(float alpha, float beta, float gamma, float tol, float small,
+                                                         float &c, float &s, float &t) {
+    if (alpha <= small || beta <= small || gamma == 0.0f) return false;
+    if (!(fabsf(gamma) * rsqrtf(alpha) * rsqrtf(beta) > tol)) return false;
+    const float zeta = __fdividef(beta - alpha, 2.0f * gamma);
+    const float az = fabsf(zeta);
+    t = az < 1e18f ? copysignf(__frcp_rn(az + sqrtf(fmaf(zeta, zeta, 1.0f))), zeta) : __fdividef(0.5f, zeta);
+    if (t == 0.0f) return false;
+    const float x = fmaf(t, t, 1.0f);
+    float y = rsqrtf(x);
+    y = y * fmaf(-0.5f * x * y, y, 1.5f);
+    c = y;
+    s = c * t;
+    return true;
+}
+
+template <>
+__device__ __forceinline__ bool jacobi_rotation_t<double>(double alpha, double beta, double gamma, double tol,
+                                                          double small, double &c, double &s, double &t) {
+    if (alpha <= small || beta <= small || gamma == 0.0) return false;
+    if (!(fabs(gamma) > tol * sqrt(alpha) * sqrt(beta))) return false;
+    const double zeta = (beta - alpha) / (2.0 * gamma);
+    const double az = fabs(zeta);
+    t = az < 1e150 ? copysign(1.0, zeta) / (az + sqrt(fma(zeta, zeta, 1.0))) : 0.5 / zeta;
+    if (t == 0.0) return false;
+    c = 1.0 / sqrt(fma(t, t, 1.0));
+    s = c * t;
+    return true;
+}
+
 // ----------------------------------------------------------- warp kernel
 template <typename T, int MR>
 __global__ void __launch_bounds__(128, 1)
@@ -257,24 +297,35 @@ __global__ void __launch_bounds__(128, 1)
 // ------------------------------------------------------------ CTA kernel
 // One block of 256 threads per matrix: 32 column pairs x 8 lanes per pair,
 // rows split across the 8 lanes; A (m x n) and V (n x n) in shared memory.
+// Column strides are multiples of 32 words, so a word's bank is its row mod
+// 32, and the four 8-lane groups of a warp start their row walk 8 rows apart:
+// every shared access of a round is conflict-free.  Column norms are cached
+// (recomputed from the columns at the start of every sweep, updated by
+// alpha - t gamma, beta + t gamma after a rotation), so a round computes one
+// dot product per pair.
 constexpr int SVJ_CTA_THREADS = 256;
 constexpr int SVJ_GROUP = 8;
 
 template <typename T>
-__global__ void __launch_bounds__(SVJ_CTA_THREADS)
+__global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
     k_gesvj_cta(int m, int n, const T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
                 T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
                 int64_t sV0, T tol, int max_sweeps, int warm_budget, int *__restrict__ fallback_out,
                 int *__restrict__ info, int *__restrict__ sweeps_out, int batch) {
     extern __shared__ __align__(16) unsigned char svsm_raw[];
     T *svsm = reinterpret_cast<T *>(svsm_raw);
-    const int lda = m | 1, ldv = n | 1;
+    const int lda = (int)round_up(m, 32), ldv = (int)round_up(n, 32);
     T *a = svsm;                      // n columns x lda
     T *v = a + (size_t)n * lda;       // n columns x ldv
     T *sig = v + (size_t)n * ldv;     // n
     T *rinv = sig + n;                // n: 1 / |rotated column j|
+    T *nrm = rinv + n;                // n: cached |a_j|^2
     const int tid = threadIdx.x, g = tid / SVJ_GROUP, gl = tid % SVJ_GROUP;
     const int N = n + (n & 1), M = N - 1;
+    // row walk of this lane: rows (gl + rot + 8 t) mod mr, t < mr / 8
+    const int rot = 8 * (g & 3);
+    const int mr = (int)round_up(m, 8), nr = (int)round_up(n, 8);
+    const int ma0 = (gl + rot) % mr, va0 = (gl + rot) % nr;
 
     for (int64_t mat = blockIdx.x; mat < batch; mat += gridDim.x) {
         const T *ag = A + mat * sA;
@@ -328,39 +379,62 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
         for (sweep = 1; sweep <= limit; sweep++) {
             total++;
             int rotated = 0;
+            // refresh the cached norms: group g takes columns g, g + 32.  The
+            // trip count is the same for every lane (the group sum shuffles
+            // across the whole warp); columns past n contribute nothing.
+            for (int j0 = 0; j0 < n; j0 += SVJ_CTA_THREADS / SVJ_GROUP) {
+                const int j = j0 + g;
+                T f = 0.f;
+                if (j < n)
+                    for (int t = 0, i = ma0; t < mr / 8; t++, i = (i + 8 < mr) ? i + 8 : i + 8 - mr)
+                        if (i < m) f = fma(a[j * lda + i], a[j * lda + i], f);
+                f = group_sum(f, SVJ_GROUP);
+                if (gl == 0 && j < n) nrm[j] = f;
+            }
+            __syncthreads();
             for (int r = 0; r < M; r++) {
                 int p = -1, q = -1;
                 if (g < N / 2) {
-                    int x = g == 0 ? M : (r + g) % M;
-                    int y = g == 0 ? r : ((r - g) % M + M) % M;
+                    int x, y;
+                    if (g == 0) {
+                        x = M;
+                        y = r;
+                    } else {
+                        x = r + g;
+                        if (x >= M) x -= M;
+                        y = r - g;
+                        if (y < 0) y += M;
+                    }
                     p = x < y ? x : y;
                     q = x < y ? y : x;
                 }
                 const bool act = q >= 0 && q < n;
-                T alpha = 0.f, beta = 0.f, gamma = 0.f;
+                T gamma = 0.f, alpha = 0.f, beta = 0.f;
                 if (act) {
-                    for (int i = gl; i < m; i += SVJ_GROUP) {
-                        T x = a[p * lda + i], y = a[q * lda + i];
-                        alpha = fma(x, x, alpha);
-                        beta = fma(y, y, beta);
-                        gamma = fma(x, y, gamma);
-                    }
+                    for (int t = 0, i = ma0; t < mr / 8; t++, i = (i + 8 < mr) ? i + 8 : i + 8 - mr)
+                        if (i < m) gamma = fma(a[p * lda + i], a[q * lda + i], gamma);
+                    alpha = nrm[p];
+                    beta = nrm[q];
                 }
-                alpha = group_sum(alpha, SVJ_GROUP);
-                beta = group_sum(beta, SVJ_GROUP);
                 gamma = group_sum(gamma, SVJ_GROUP);
-                T c, s;
-                if (act && jacobi_rotation<T>(alpha, beta, gamma, tol_eff, small, c, s)) {
+                T c, sn, tn;
+                if (act && jacobi_rotation_t<T>(alpha, beta, gamma, tol_eff, small, c, sn, tn)) {
                     rotated = 1;
-                    for (int i = gl; i < m; i += SVJ_GROUP) {
+                    for (int t = 0, i = ma0; t < mr / 8; t++, i = (i + 8 < mr) ? i + 8 : i + 8 - mr) {
+                        if (i >= m) continue;
                         T x = a[p * lda + i], y = a[q * lda + i];
-                        a[p * lda + i] = fma(c, x, -s * y);
-                        a[q * lda + i] = fma(s, x, c * y);
+                        a[p * lda + i] = fma(c, x, -sn * y);
+                        a[q * lda + i] = fma(sn, x, c * y);
                     }
-                    for (int i = gl; i < n; i += SVJ_GROUP) {
+                    for (int t = 0, i = va0; t < nr / 8; t++, i = (i + 8 < nr) ? i + 8 : i + 8 - nr) {
+                        if (i >= n) continue;
                         T x = v[p * ldv + i], y = v[q * ldv + i];
-                        v[p * ldv + i] = fma(c, x, -s * y);
-                        v[q * ldv + i] = fma(s, x, c * y);
+                        v[p * ldv + i] = fma(c, x, -sn * y);
+                        v[q * ldv + i] = fma(sn, x, c * y);
+                    }
+                    if (gl == 0) {
+                        nrm[p] = fma(-tn, gamma, alpha);
+                        nrm[q] = fma(tn, gamma, beta);
                     }
                 }
                 __syncthreads();
@@ -471,7 +545,7 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS)
 
 template <typename T>
 static size_t svj_cta_smem(int m, int n) {
-    return sizeof(T) * ((size_t)n * (m | 1) + (size_t)n * (n | 1) + 2 * (size_t)n) + 16;
+    return sizeof(T) * ((size_t)n * round_up(m, 32) + (size_t)n * round_up(n, 32) + 3 * (size_t)n) + 16;
 }
 
 // ---------------------------------------------------------------- rank

@@ -198,43 +198,74 @@ __device__ void sm_transpose(int n, const float *A, float *D) {
 
 // X = (I - S)^{-1} by Gauss-Jordan without pivoting on [I - S | I].  The
 // symmetric part of I - S is I, and so is that of every Schur complement, so
-// every pivot has modulus >= 1 and no pivoting is needed.  L is scratch.
-__device__ void sm_cayley_inverse(int n, const float *o, float *L, float *X, float *fcol) {
-    const int tid = threadIdx.x;
-    for (int e = tid; e < n * n; e += WS_T) {
-        const int i = e % n, j = e / n;
-        float s = 0.0f;
-        if (i < j) s = o[upper_index(i, j, n)];
-        else if (i > j) s = -o[upper_index(j, i, n)];
-        L[j * WS_LD + i] = (i == j ? 1.0f : 0.0f) - s;
-        X[j * WS_LD + i] = i == j ? 1.0f : 0.0f;
-    }
-    __syncthreads();
-    const int row = tid & 63, c0 = tid >> 6;  // thread: one row, columns c0 + 4 t of [L | X]
-    for (int k = 0; k < n; k++) {
-        const float inv = 1.0f / L[k * WS_LD + k];
-        if (tid < n) fcol[tid] = L[k * WS_LD + tid];
-        __syncthreads();
-        for (int c = tid; c < 2 * n; c += WS_T) {
-            if (c < n) {
-                if (c > k) L[c * WS_LD + k] *= inv;
+// every pivot has modulus >= 1 and no pivoting is needed.  The 64 x 128
+// augmented matrix lives in registers: thread t owns rows 4 (t % 16) .. +3 and
+// columns 8 (t / 16) .. +7 (columns 64.. are the X half; rows and columns past
+// n are identity padding).  Step k: the owners of column k publish it, the
+// owners of row k scale it by the pivot and publish it, every thread updates
+// its block.  pcol / prow are double-buffered by the parity of k, so two
+// barriers per step suffice.  X is left in shared memory (stride WS_LD).
+struct GJBuf {
+    float pcol[2][64];
+    float prow[2][128];
+};
+
+__device__ void sm_cayley_inverse(int n, const float *o, float *X, GJBuf &gb) {
+    const int t = threadIdx.x, r0 = (t & 15) * 4, c0 = (t >> 4) * 8;
+    float m[4][8];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            const int r = r0 + a, c = c0 + b;
+            float v;
+            if (c < 64) {
+                v = r == c ? 1.0f : 0.0f;
+                if (r < n && c < n && r != c) v = r < c ? -o[upper_index(r, c, n)] : o[upper_index(c, r, n)];
             } else {
-                X[(c - n) * WS_LD + k] *= inv;
+                v = r == c - 64 ? 1.0f : 0.0f;
             }
+            m[a][b] = v;
         }
-        __syncthreads();
-        if (row < n && row != k) {
-            const float f = fcol[row];
-            for (int c = c0; c < 2 * n; c += 4) {
-                if (c < n) {
-                    if (c > k) L[c * WS_LD + row] = fmaf(-f, L[c * WS_LD + k], L[c * WS_LD + row]);
-                } else {
-                    X[(c - n) * WS_LD + row] = fmaf(-f, X[(c - n) * WS_LD + k], X[(c - n) * WS_LD + row]);
+    for (int kk = 0; kk < n; kk += 8) {
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            const int k = kk + b;
+            if (k >= n) break;
+            const int par = k & 1;
+            if (c0 == kk) {
+#pragma unroll
+                for (int a = 0; a < 4; a++) gb.pcol[par][r0 + a] = m[a][b];
+            }
+            __syncthreads();
+            if (r0 == (k & ~3)) {
+                const float inv = 1.0f / gb.pcol[par][k];
+#pragma unroll
+                for (int bb = 0; bb < 8; bb++) {
+                    m[b & 3][bb] *= inv;
+                    gb.prow[par][c0 + bb] = m[b & 3][bb];
                 }
             }
+            __syncthreads();
+            float pr[8];
+#pragma unroll
+            for (int bb = 0; bb < 8; bb++) pr[bb] = gb.prow[par][c0 + bb];
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                if (r0 + a == k) continue;
+                const float f = gb.pcol[par][r0 + a];
+#pragma unroll
+                for (int bb = 0; bb < 8; bb++) m[a][bb] = fmaf(-f, pr[bb], m[a][bb]);
+            }
         }
-        __syncthreads();
     }
+    if (c0 >= 64) {
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 8; b++) X[(c0 - 64 + b) * WS_LD + r0 + a] = m[a][b];
+    }
+    __syncthreads();
 }
 
 // V0 = Vb (2 X - I) = 2 Vb X - Vb
@@ -318,7 +349,8 @@ __device__ void sm_assign(int n, const float *C, int *perm, float *sgn, int *rbe
 
 struct LossSmem {
     int perm[64], rbest[64], cbest[64], rdone[64], cdone[64], wi[8];
-    float sgn[64], fcol[64], wv[8], red[8];
+    float sgn[64], wv[8], red[8];
+    GJBuf gj;
 };
 
 // Loss + gradient w.r.t. the network outputs for one matrix per block.
@@ -341,7 +373,7 @@ __global__ void __launch_bounds__(WS_T)
     }
     __syncthreads();
     sm_transpose(n, Vb, VbT);
-    sm_cayley_inverse(n, out + (int64_t)b * P, L, X, ls.fcol);
+    sm_cayley_inverse(n, out + (int64_t)b * P, X, ls.gj);
     sm_frame(n, Vb, X, V0);
     sm_transpose(n, V0, T1);
     sm_mm(n, T1, Vt, L, 1.0f);  // C = V0^T V
@@ -377,24 +409,26 @@ __global__ void __launch_bounds__(WS_T)
     }
 }
 
-// V0 for one matrix per block
+// V0 for a batch: persistent blocks, Vb loaded once per block
 __global__ void __launch_bounds__(WS_T)
     k_ws_frame(int n, int P, const float *__restrict__ out, const float *__restrict__ Vbase, float *__restrict__ V0g,
                int64_t sV0, int batch) {
     extern __shared__ __align__(16) float wsm[];
-    float *L = wsm, *X = L + WS_MAT, *Vb = X + WS_MAT, *V0 = Vb + WS_MAT;
-    __shared__ float fcol[64];
-    const int b = blockIdx.x, tid = threadIdx.x;
-    if (b >= batch) return;
+    float *X = wsm, *Vb = X + WS_MAT, *V0 = Vb + WS_MAT;
+    __shared__ GJBuf gb;
+    const int tid = threadIdx.x;
     for (int e = tid; e < n * n; e += WS_T) Vb[(e / n) * WS_LD + e % n] = Vbase[e];
     __syncthreads();
-    sm_cayley_inverse(n, out + (int64_t)b * P, L, X, fcol);
-    sm_frame(n, Vb, X, V0);
-    for (int e = tid; e < n * n; e += WS_T) V0g[(int64_t)b * sV0 + e] = V0[(e / n) * WS_LD + e % n];
+    for (int b = blockIdx.x; b < batch; b += gridDim.x) {
+        sm_cayley_inverse(n, out + (int64_t)b * P, X, gb);
+        sm_frame(n, Vb, X, V0);
+        for (int e = tid; e < n * n; e += WS_T) V0g[(int64_t)b * sV0 + e] = V0[(e / n) * WS_LD + e % n];
+        __syncthreads();
+    }
 }
 
 constexpr size_t LOSS_SMEM = 7 * WS_MAT * sizeof(float);
-constexpr size_t FRAME_SMEM = 4 * WS_MAT * sizeof(float);
+constexpr size_t FRAME_SMEM = 3 * WS_MAT * sizeof(float);
 
 unsigned grid_for(int64_t n, int threads) {
     int64_t g = (n + threads - 1) / threads;
@@ -691,7 +725,8 @@ GBLA_API gbla_status gbla_wsnet_predict(gbla_wsnet *w, const float *A, int64_t s
     for (int b0 = 0; b0 < batch; b0 += w->maxb) {
         const int nb = batch - b0 < w->maxb ? batch - b0 : w->maxb;
         WS_TRY(forward(w, A + (int64_t)b0 * sA, sA, nullptr, nb, false, st));
-        k_ws_frame<<<(unsigned)nb, WS_T, FRAME_SMEM, st>>>(w->n, w->P, w->out, w->vbase, V0 + (int64_t)b0 * sV0, sV0,
+        const int grid = nb < sm_count() * 4 ? nb : sm_count() * 4;
+        k_ws_frame<<<(unsigned)grid, WS_T, FRAME_SMEM, st>>>(w->n, w->P, w->out, w->vbase, V0 + (int64_t)b0 * sV0, sV0,
                                                            nb);
         WS_TRY(launch_status());
     }
