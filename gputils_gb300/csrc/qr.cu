@@ -67,6 +67,7 @@ __device__ __forceinline__ T reduce_scatter32(T (&p)[32], int lane) {
 template <typename T, int R>
 struct QrWarp {
     T a[R][32];  // rows lane + 32 t, columns 0..31
+    T dinv;      // 1 / R_ll in lane l < n (set by factor)
     int lane;
 
     __device__ __forceinline__ int row(int t) const { return lane + 32 * t; }
@@ -74,6 +75,7 @@ struct QrWarp {
     // Householder QR in registers; tau written to tau_s[k] (shared, per warp).
     __device__ __forceinline__ int factor(int m, int n, T *tau_s) {
         int rank_fail = 0;
+        T rdiag = T(0);  // R_ll of this lane (warp-uniform value of step l)
 #pragma unroll
         for (int k = 0; k < 32; k++) {
             if (k < n) {
@@ -84,8 +86,10 @@ struct QrWarp {
                 x2 = warp_sum(x2);
                 const T alpha = shfl(a[0][k], k);
                 T tau = T(0);
+                if (lane == k) rdiag = alpha;
                 if (x2 > T(0)) {
                     const T beta = -copysign(dev_sqrt<T>(fma(alpha, alpha, x2)), alpha);
+                    if (lane == k) rdiag = beta;
                     tau = (beta - alpha) / beta;
                     const T scal = T(1) / (alpha - beta);
 #pragma unroll
@@ -123,6 +127,8 @@ struct QrWarp {
                 if (shfl(a[0][k], k) == T(0) && rank_fail == 0) rank_fail = k + 1;
             }
         }
+        // reciprocal of this lane's diagonal entry, once for every triangular solve
+        dinv = (lane < n && rdiag != T(0)) ? T(1) / rdiag : T(0);
         __syncwarp();
         return rank_fail;
     }
@@ -161,7 +167,7 @@ struct QrWarp {
 #pragma unroll
         for (int j = 31; j >= 0; j--) {
             if (j < n) {
-                T zj = shfl(y / a[0][j], j);  // lane j holds y_j and R_jj
+                T zj = shfl(y * dinv, j);  // lane j holds y_j and 1 / R_jj
                 if (lane == j) z = zj;
                 if (lane < j) y = fma(-a[0][j], zj, y);
             }
@@ -177,7 +183,7 @@ struct QrWarp {
             if (j < n) {
                 T part = lane < j ? a[0][j] * h : T(0);  // R_ij h_i, i < j
                 T s = warp_sum(part);
-                T hj = (g - s) / a[0][j];
+                T hj = shfl((g - s) * dinv, j);
                 if (lane == j) h = hj;
             }
         }
@@ -197,20 +203,26 @@ __device__ __forceinline__ float refine_ls(const QrWarp<float, R> &q, const floa
 #pragma unroll
     for (int t = 0; t < R; t++) { rh[t] = 0.f; rl[t] = 0.f; }
     for (int it = 0; it <= refine; it++) {
-        // f = b - r - A x  (rows)
+        // f = b - r - A x (rows).  At it == 1, r is the residual of x adopted
+        // at it == 0 and x has not moved, so f vanishes to ~2^-48: skip it
+        // (and d = Q^T f with it).
+        const bool fzero = it == 1;
         ff f[R];
 #pragma unroll
         for (int t = 0; t < R; t++) {
-            f[t].h = b[t]; f[t].l = 0.f;
-            ff_add(f[t], -rh[t], -rl[t]);
+            f[t].h = fzero ? 0.f : b[t];
+            f[t].l = 0.f;
+            if (!fzero) ff_add(f[t], -rh[t], -rl[t]);
         }
-        for (int j = 0; j < n; j++) {
-            float xjh = shfl(xh, j), xjl = shfl(xl, j);
+        if (!fzero) {
+            for (int j = 0; j < n; j++) {
+                float xjh = shfl(xh, j), xjl = shfl(xl, j);
 #pragma unroll
-            for (int t = 0; t < R; t++) {
-                int r = lane + 32 * t;
-                float aij = r < m ? A0[j * LDM + r] : 0.f;
-                ff_fma(f[t], -aij, xjh, xjl);
+                for (int t = 0; t < R; t++) {
+                    int r = lane + 32 * t;
+                    float aij = r < m ? A0[j * LDM + r] : 0.f;
+                    ff_fma(f[t], -aij, xjh, xjl);
+                }
             }
         }
         if (it == 0) {
@@ -222,41 +234,52 @@ __device__ __forceinline__ float refine_ls(const QrWarp<float, R> &q, const floa
             }
             continue;
         }
-        // g = -A^T r (lane j keeps column j)
+        // g = -A^T r (lane j keeps column j); eight columns per reduce-scatter
         float gj = 0.f;
-        for (int j = 0; j < n; j++) {
-            ff acc = {0.f, 0.f};
+        for (int j0 = 0; j0 < n; j0 += 8) {
+            ff acc[8];
 #pragma unroll
-            for (int t = 0; t < R; t++) {
-                int r = lane + 32 * t;
-                float aij = r < m ? A0[j * LDM + r] : 0.f;
-                ff_fma(acc, aij, rh[t], rl[t]);
+            for (int c = 0; c < 8; c++) {
+                acc[c].h = 0.f;
+                acc[c].l = 0.f;
+                if (j0 + c < n) {
+#pragma unroll
+                    for (int t = 0; t < R; t++) {
+                        int r = lane + 32 * t;
+                        float aij = r < m ? A0[(j0 + c) * LDM + r] : 0.f;
+                        ff_fma(acc[c], aij, rh[t], rl[t]);
+                    }
+                }
             }
-            acc = ff_warp_sum(acc);
-            if (lane == j) gj = -(acc.h + acc.l);
+            const ff tot = ff_reduce_scatter8(acc, lane);
+            const float gs = shfl(tot.h + tot.l, 4 * (lane & 7));
+            if ((lane >> 3) == (j0 >> 3)) gj = -gs;
         }
+        float h = q.forward_solve_rt(n, gj);
         float fr[R];
 #pragma unroll
-        for (int t = 0; t < R; t++) fr[t] = f[t].h + f[t].l;
-        float h = q.forward_solve_rt(n, gj);
-        q.apply_qt(n, tau_s, fr);                       // d = Q^T f
+        for (int t = 0; t < R; t++) fr[t] = fzero ? 0.f : f[t].h + f[t].l;
+        if (!fzero) q.apply_qt(n, tau_s, fr);           // d = Q^T f
         float dx = q.back_solve(n, lane < n ? fr[0] - h : 0.f);
-        float z[R];
+        if (it < refine) {
+            // dr = Q [h; d2], needed only by a further step
+            float z[R];
 #pragma unroll
-        for (int t = 0; t < R; t++) z[t] = (lane + 32 * t) < n ? h : fr[t];
-        q.apply_q(n, tau_s, z);                         // dr = Q [h; d2]
+            for (int t = 0; t < R; t++) z[t] = (lane + 32 * t) < n ? h : fr[t];
+            q.apply_q(n, tau_s, z);
+#pragma unroll
+            for (int t = 0; t < R; t++) {
+                float s, e;
+                two_sum(rh[t], z[t], s, e);
+                float l = rl[t] + e;
+                rh[t] = s + l; rl[t] = l - (rh[t] - s);
+            }
+        }
         {
             float s, e;
             two_sum(xh, dx, s, e);
             float l = xl + e;
             xh = s + l; xl = l - (xh - s);
-        }
-#pragma unroll
-        for (int t = 0; t < R; t++) {
-            float s, e;
-            two_sum(rh[t], z[t], s, e);
-            float l = rl[t] + e;
-            rh[t] = s + l; rl[t] = l - (rh[t] - s);
         }
     }
     return xh + xl;

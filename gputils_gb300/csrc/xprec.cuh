@@ -54,4 +54,38 @@ __device__ __forceinline__ ff ff_warp_sum(ff a) {
     return ff_norm(a);
 }
 
+// Reduce-scatter of 8 double-FP32 slots across the warp (9 exchanges instead
+// of 8 full butterflies): on return every lane holds the warp-wide total of
+// slot (lane >> 2) & 7, i.e. lanes 4 s .. 4 s + 3 hold slot s.
+__device__ __forceinline__ ff ff_reduce_scatter8(const ff (&p)[8], int lane) {
+    ff q[4];
+    const bool b4 = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const ff mine = b4 ? p[i + 4] : p[i], other = b4 ? p[i] : p[i + 4];
+        q[i] = mine;
+        ff_add(q[i], shfl_xor(other.h, 16), shfl_xor(other.l, 16));
+    }
+    const bool b3 = lane & 8;
+    ff r[2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const ff mine = b3 ? q[i + 2] : q[i], other = b3 ? q[i] : q[i + 2];
+        r[i] = mine;
+        ff_add(r[i], shfl_xor(other.h, 8), shfl_xor(other.l, 8));
+    }
+    const bool b2 = lane & 4;
+    ff s = b2 ? r[1] : r[0];
+    {
+        const ff other = b2 ? r[0] : r[1];
+        ff_add(s, shfl_xor(other.h, 4), shfl_xor(other.l, 4));
+    }
+#pragma unroll
+    for (int o = 2; o > 0; o >>= 1) {
+        const float oh = shfl_xor(s.h, o), ol = shfl_xor(s.l, o);
+        ff_add(s, oh, ol);
+    }
+    return ff_norm(s);
+}
+
 }  // namespace gbla
