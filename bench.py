@@ -70,6 +70,7 @@ def parse_args(argv=None):
     ap.add_argument("--no-reference-library", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
     ap.add_argument("--peaks", action="store_true", help="print the measured FFMA / DFMA rates and exit")
+    ap.add_argument("--no-autotune", action="store_true", help="d3: keep the plan's default launch configuration")
     ap.add_argument("--ws-pairs", type=int, default=200_000, help="d5: (A, V) training pairs of the warm-start net")
     ap.add_argument("--ws-epochs", type=int, default=20, help="d5: training epochs of the warm-start net")
     return ap.parse_args(argv)
@@ -565,6 +566,14 @@ def _ragged_bytes(n, nrhs, elem):
     return int((elem * (n * n + n * (n + 1) // 2 + 2 * n * nrhs)).sum())
 
 
+class RaggedCfg(C.Structure):
+    _fields_ = [("bucket_width", C.c_int), ("large_threads", C.c_int), ("fork_small", C.c_int)]
+
+    def as_dict(self):
+        return {"bucket_width": self.bucket_width, "large_threads": self.large_threads,
+                "fork_small": self.fork_small}
+
+
 def run_ours_d3(args, dev, st, L, rank, world, dist):
     """One gbla_{s,d}posv_ragged call per step on 20000 mixed systems,
     captured once per step buffer in a CUDA graph and replayed."""
@@ -586,6 +595,17 @@ def run_ours_d3(args, dev, st, L, rank, world, dist):
     fn = L.gbla_sposv_ragged if dt == np.float32 else L.gbla_dposv_ragged
     A0 = torch.from_numpy(A).to(dev)
     B0 = torch.from_numpy(B).to(dev)
+    # launch configuration: the plan's autotuner on this batch (set-up, untimed)
+    cfg = RaggedCfg()
+    _lib.check(L.gbla_ragged_plan_get_config(plan, C.byref(cfg)), "get config")
+    tuning = {"default": cfg.as_dict()}
+    if not args.no_autotune:
+        best, best_ms = RaggedCfg(), C.c_float()
+        tune = L.gbla_sragged_autotune if dt == np.float32 else L.gbla_dragged_autotune
+        _lib.check(tune(plan, A0.data_ptr(), B0.data_ptr(), refine, 3, C.byref(best), C.byref(best_ms), st),
+                   "autotune")
+        tuning.update({"chosen": best.as_dict(), "chosen_ms": best_ms.value, "candidates": 24})
+        cfg = best
     nsteps = args.warmup + args.steps
     As = [A0.clone() for _ in range(nsteps)]
     Bs = [B0.clone() for _ in range(nsteps)]
@@ -667,12 +687,14 @@ def run_ours_d3(args, dev, st, L, rank, world, dist):
     t = elapsed_max / args.steps
     bytes_ = _ragged_bytes(n, nrhs, np.dtype(dt).itemsize)
     ach = bytes_ / t / 1e9
-    launches = 4 if dt == np.float32 else 4
+    large = n[n > 32]
+    buckets = min(8, len(np.unique(np.ceil((large - 32) / cfg.bucket_width)))) if len(large) else 0
+    launches = buckets + sum(1 for lo, hi in ((0, 8), (8, 16), (16, 32)) if ((n > lo) & (n <= hi)).any())
     return {
         "metric": metric_name("d3"), "value": units_all / elapsed_max, "unit": "matrices/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded)",
-        "config": dict(workload_config("d3", args), refine_steps=refine),
+        "config": dict(workload_config("d3", args), refine_steps=refine, launch_config=tuning),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": ach / pk["hbm_gbs"], "traffic": traffic_for("ragged_d3_" + args.dtype),
                      "kernel": "posv_ragged (all kernels of one call)", "algorithmic_bytes_per_launch": bytes_},

@@ -11,13 +11,20 @@
 //                identity, which leaves their factor and solution unchanged.
 //   * n > 32   : one block per system, shared-memory factor, one warp per
 //                right-hand side; blocks are issued largest system first.
-// The two families run on a forked stream pair (graph-capturable fork/join).
+// The large class is cut into buckets of similar n (each launch sizes its
+// shared memory for its own largest system, so small members of the class are
+// not run at the occupancy of n = 128), spread over forked streams.  Bucket
+// width, threads per block and whether the small classes get their own stream
+// form the plan's launch configuration; gbla_{s,d}ragged_autotune times the
+// candidates on the caller's batch and keeps the fastest.  All forks and joins
+// are event-based, so a call can be captured in a CUDA graph.
 //
 // Precision: the factorisation and the triangular solves run in FP32; each
 // refinement step recomputes r = b - A x from the original, full symmetric A
 // (lower and upper triangles) in extended precision -- double-FP32 for float
 // data, FP64 for double data -- and adds the FP32 correction.
 #include <algorithm>
+#include <new>
 #include <vector>
 #include "chol_common.cuh"
 #include "xprec.cuh"
@@ -27,21 +34,27 @@ struct RaggedSys {
     int n, nrhs, orig, pad;
 };
 
+constexpr int RG_MAX_BUCKETS = 8;
+constexpr int RG_STREAMS = 3;  // forked streams: small classes, two for large buckets
+
 struct gbla_ragged_plan {
     int device = -1;
     int count = 0;
     int first[4] = {0, 0, 0, 0};   // classes: NB 8, NB 16, NB 32, large
     int num[4] = {0, 0, 0, 0};
     int max_n_large = 0;
+    gbla_ragged_config cfg = {96, 256, 1};
+    // large-class buckets for cfg.bucket_width (contiguous, largest n first)
+    int nb = 0, b_first[RG_MAX_BUCKETS] = {}, b_num[RG_MAX_BUCKETS] = {}, b_nmax[RG_MAX_BUCKETS] = {};
+    int64_t a_extent = 0, b_extent = 0;  // arena sizes in elements
+    std::vector<int> large_n;            // n of the large class, in plan order
     RaggedSys *d_sys = nullptr;
-    cudaStream_t aux = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t aux[RG_STREAMS] = {};
+    cudaEvent_t fork = nullptr, join[RG_STREAMS] = {};
 };
 
 namespace gbla {
 
-constexpr int RG_LARGE_THREADS = 256;
-constexpr int RG_LARGE_WARPS = RG_LARGE_THREADS / 32;
 
 // ------------------------------------------------------------ small systems
 template <typename T, int NB>
@@ -123,17 +136,17 @@ __global__ void __launch_bounds__(128, 1)
 
 // ------------------------------------------------------------ large systems
 template <typename T>
-__host__ __device__ inline size_t ragged_large_smem(int nmax) {
+__host__ __device__ inline size_t ragged_large_smem(int nmax, int warps) {
     const int ld = cta_ld(nmax);
-    // float factor (n x ld) + float dinv (n) + float work (8 x n) + T x (8 x n)
-    return sizeof(float) * ((size_t)nmax * ld + nmax + (size_t)RG_LARGE_WARPS * nmax) +
-           sizeof(T) * (size_t)RG_LARGE_WARPS * nmax + 64;
+    // float factor (n x ld) + float dinv (n) + float work (warps x n) + T x (warps x n)
+    return sizeof(float) * ((size_t)nmax * ld + nmax + (size_t)warps * nmax) + sizeof(T) * (size_t)warps * nmax + 64;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(RG_LARGE_THREADS, 1)
+template <typename T, int THREADS>
+__global__ void __launch_bounds__(THREADS)
     k_ragged_large(const RaggedSys *__restrict__ sys, int first, int nmax, const T *__restrict__ A_in,
                    T *__restrict__ A, T *__restrict__ B, int *__restrict__ info, int refine) {
+    constexpr int RG_LARGE_WARPS = THREADS / 32;
     extern __shared__ __align__(16) unsigned char rsm[];
     const RaggedSys s = sys[first + blockIdx.x];
     const int n = s.n, nrhs = s.nrhs, ld = cta_ld(n);
@@ -243,6 +256,43 @@ __global__ void __launch_bounds__(RG_LARGE_THREADS, 1)
         for (int i = j + lane; i < n; i += 32) aw[(int64_t)j * n + i] = (T)a[(int64_t)j * ld + i];
 }
 
+// Bucket the large class (plan order: largest n first) by cfg.bucket_width:
+// bucket boundaries at 32 + w, 32 + 2w, ...; a bucket's smem is sized for its
+// first (largest) system.
+static void ragged_buckets(gbla_ragged_plan *p) {
+    p->nb = 0;
+    const int nl = p->num[3];
+    int i = 0;
+    while (i < nl && p->nb < RG_MAX_BUCKETS) {
+        const int top = p->large_n[i];
+        // bucket of top: (lo, hi] with hi - 32 a multiple of w
+        const int w = p->cfg.bucket_width;
+        const int hi = 32 + ((top - 32 + w - 1) / w) * w;
+        const int lo = (p->nb == RG_MAX_BUCKETS - 1) ? 32 : hi - w;
+        int j = i;
+        while (j < nl && p->large_n[j] > lo) j++;
+        p->b_first[p->nb] = p->first[3] + i;
+        p->b_num[p->nb] = j - i;
+        p->b_nmax[p->nb] = top;
+        p->nb++;
+        i = j;
+    }
+}
+
+template <typename T, int THREADS>
+static gbla_status launch_large(const gbla_ragged_plan *p, int b, T *A, T *B, int *info, int refine,
+                                cudaStream_t st) {
+    const size_t smem = ragged_large_smem<T>(p->b_nmax[b], THREADS / 32);
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_ragged_large<T, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return from_cuda(e);
+    }
+    k_ragged_large<T, THREADS><<<p->b_num[b], THREADS, smem, st>>>(p->d_sys, p->b_first[b], p->b_nmax[b], A, A, B,
+                                                                    info, refine);
+    return launch_status();
+}
+
 template <typename T>
 static gbla_status ragged_launch(const gbla_ragged_plan *p, T *A, T *B, int *info, int refine, cudaStream_t st) {
     if (!p || refine < 0) return GBLA_INVALID_VALUE;
@@ -252,23 +302,27 @@ static gbla_status ragged_launch(const gbla_ragged_plan *p, T *A, T *B, int *inf
     cudaGetDevice(&dev);
     if (dev != p->device) return GBLA_INVALID_VALUE;
     cudaError_t e;
-    const bool fork = p->num[3] > 0 && (p->num[0] + p->num[1] + p->num[2]) > 0;
-    cudaStream_t small_st = fork ? p->aux : st;
-    if (fork) {
+    const int nsmall = p->num[0] + p->num[1] + p->num[2];
+    // streams: small classes on aux[0] when forked; large buckets alternate
+    // between the caller's stream and aux[1], aux[2]
+    const bool fork_small = p->cfg.fork_small && nsmall > 0 && p->nb > 0;
+    const int large_streams = p->nb < 3 ? p->nb : 3;
+    bool used[RG_STREAMS] = {fork_small, large_streams > 1, large_streams > 2};
+    if (used[0] || used[1] || used[2]) {
         if ((e = cudaEventRecord(p->fork, st)) != cudaSuccess) return from_cuda(e);
-        if ((e = cudaStreamWaitEvent(p->aux, p->fork, 0)) != cudaSuccess) return from_cuda(e);
+        for (int k = 0; k < RG_STREAMS; k++)
+            if (used[k] && (e = cudaStreamWaitEvent(p->aux[k], p->fork, 0)) != cudaSuccess) return from_cuda(e);
     }
-    if (p->num[3] > 0) {
-        const size_t smem = ragged_large_smem<T>(p->max_n_large);
-        if (smem > 48 * 1024) {
-            e = cudaFuncSetAttribute(k_ragged_large<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return from_cuda(e);
-        }
-        k_ragged_large<T><<<p->num[3], RG_LARGE_THREADS, smem, st>>>(p->d_sys, p->first[3], p->max_n_large, A, A, B,
-                                                                      info, refine);
-        gbla_status s = launch_status();
+    for (int b = 0; b < p->nb; b++) {
+        const int sidx = large_streams > 0 ? b % large_streams : 0;
+        cudaStream_t ls = sidx == 0 ? st : p->aux[sidx];
+        gbla_status s;
+        if (p->cfg.large_threads == 128) s = launch_large<T, 128>(p, b, A, B, info, refine, ls);
+        else if (p->cfg.large_threads == 512) s = launch_large<T, 512>(p, b, A, B, info, refine, ls);
+        else s = launch_large<T, 256>(p, b, A, B, info, refine, ls);
         if (s != GBLA_SUCCESS) return s;
     }
+    cudaStream_t small_st = fork_small ? p->aux[0] : st;
     const int gpw[3] = {4, 2, 1};
     for (int c = 0; c < 3; c++) {
         if (p->num[c] == 0) continue;
@@ -282,11 +336,92 @@ static gbla_status ragged_launch(const gbla_ragged_plan *p, T *A, T *B, int *inf
         gbla_status s = launch_status();
         if (s != GBLA_SUCCESS) return s;
     }
-    if (fork) {
-        if ((e = cudaEventRecord(p->join, p->aux)) != cudaSuccess) return from_cuda(e);
-        if ((e = cudaStreamWaitEvent(st, p->join, 0)) != cudaSuccess) return from_cuda(e);
+    for (int k = 0; k < RG_STREAMS; k++) {
+        if (!used[k]) continue;
+        if ((e = cudaEventRecord(p->join[k], p->aux[k])) != cudaSuccess) return from_cuda(e);
+        if ((e = cudaStreamWaitEvent(st, p->join[k], 0)) != cudaSuccess) return from_cuda(e);
     }
     return GBLA_SUCCESS;
+}
+
+static bool config_valid(const gbla_ragged_config &c) {
+    return (c.bucket_width == 16 || c.bucket_width == 32 || c.bucket_width == 48 || c.bucket_width == 96) &&
+           (c.large_threads == 128 || c.large_threads == 256 || c.large_threads == 512) &&
+           (c.fork_small == 0 || c.fork_small == 1);
+}
+
+// Time every candidate configuration on the caller's batch.  A and B are
+// copied to scratch arenas; every trial runs on fresh copies and the
+// caller's arrays are left as they were.
+template <typename T>
+static gbla_status ragged_autotune(gbla_ragged_plan *p, const T *A, const T *B, int refine, int reps,
+                                   gbla_ragged_config *best_out, float *best_ms, cudaStream_t st) {
+    if (!p || refine < 0 || reps < 1) return GBLA_INVALID_VALUE;
+    if (p->count == 0) {
+        if (best_out) *best_out = p->cfg;
+        if (best_ms) *best_ms = 0.f;
+        return GBLA_SUCCESS;
+    }
+    if (!A || !B) return GBLA_INVALID_VALUE;
+    T *sa = nullptr, *sb = nullptr, *wa = nullptr, *wb = nullptr;
+    int *sinfo = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const size_t abytes = sizeof(T) * (size_t)(p->a_extent > 0 ? p->a_extent : 1);
+    const size_t bbytes = sizeof(T) * (size_t)(p->b_extent > 0 ? p->b_extent : 1);
+    cudaError_t e = cudaMalloc(&sa, abytes);
+    if (e == cudaSuccess) e = cudaMalloc(&sb, bbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&wa, abytes);
+    if (e == cudaSuccess) e = cudaMalloc(&wb, bbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&sinfo, sizeof(int) * (size_t)p->count);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sa, A, abytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sb, B, bbytes, cudaMemcpyDeviceToDevice, st);
+    gbla_status status = from_cuda(e);
+    const gbla_ragged_config saved = p->cfg;
+    gbla_ragged_config best = saved;
+    float best_t = 3.4e38f;
+    const int widths[4] = {96, 48, 32, 16}, threads[3] = {128, 256, 512};
+    for (int wi = 0; wi < 4 && status == GBLA_SUCCESS; wi++)
+        for (int ti = 0; ti < 3 && status == GBLA_SUCCESS; ti++)
+            for (int f = 0; f < 2 && status == GBLA_SUCCESS; f++) {
+                p->cfg = {widths[wi], threads[ti], f};
+                ragged_buckets(p);
+                float t_min = 3.4e38f;
+                for (int r = 0; r <= reps && status == GBLA_SUCCESS; r++) {  // r = 0: warm-up
+                    e = cudaMemcpyAsync(wa, sa, abytes, cudaMemcpyDeviceToDevice, st);
+                    if (e == cudaSuccess) e = cudaMemcpyAsync(wb, sb, bbytes, cudaMemcpyDeviceToDevice, st);
+                    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+                    if (e != cudaSuccess) { status = from_cuda(e); break; }
+                    status = ragged_launch<T>(p, wa, wb, sinfo, refine, st);
+                    if (status != GBLA_SUCCESS) break;
+                    e = cudaEventRecord(e1, st);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                    if (e != cudaSuccess) { status = from_cuda(e); break; }
+                    if (r > 0 && ms < t_min) t_min = ms;
+                }
+                if (status == GBLA_SUCCESS && t_min < best_t) {
+                    best_t = t_min;
+                    best = p->cfg;
+                }
+            }
+    p->cfg = status == GBLA_SUCCESS ? best : saved;
+    ragged_buckets(p);
+    cudaStreamSynchronize(st);
+    if (sa) cudaFree(sa);
+    if (sb) cudaFree(sb);
+    if (wa) cudaFree(wa);
+    if (wb) cudaFree(wb);
+    if (sinfo) cudaFree(sinfo);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (status == GBLA_SUCCESS) {
+        if (best_out) *best_out = best;
+        if (best_ms) *best_ms = best_t;
+    }
+    return status;
 }
 
 }  // namespace gbla
@@ -311,25 +446,30 @@ GBLA_API gbla_status gbla_ragged_plan_create(const int64_t *a_offsets, const int
         if (x.n != y.n) return x.n > y.n;
         return x.nrhs > y.nrhs;
     });
-    auto *p = new gbla_ragged_plan();
+    auto *p = new (std::nothrow) gbla_ragged_plan();
+    if (!p) return GBLA_CUDA_ERROR;
     p->count = count;
-    for (int i = 0; i < count; i++) p->num[cls(v[i].n)]++;
+    for (int i = 0; i < count; i++) {
+        p->num[cls(v[i].n)]++;
+        p->a_extent = std::max(p->a_extent, v[i].a_off + (int64_t)v[i].n * v[i].n);
+        p->b_extent = std::max(p->b_extent, v[i].b_off + (int64_t)v[i].n * v[i].nrhs);
+    }
     p->first[0] = 0;
     for (int c = 1; c < 4; c++) p->first[c] = p->first[c - 1] + p->num[c - 1];
     p->max_n_large = p->num[3] > 0 ? v[p->first[3]].n : 0;
+    for (int i = p->first[3]; i < count; i++) p->large_n.push_back(v[i].n);
+    ragged_buckets(p);
     cudaError_t e = cudaGetDevice(&p->device);
     if (e == cudaSuccess && count > 0) e = cudaMalloc(&p->d_sys, sizeof(RaggedSys) * (size_t)count);
     if (e == cudaSuccess && count > 0)
         e = cudaMemcpy(p->d_sys, v.data(), sizeof(RaggedSys) * (size_t)count, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking);
+    for (int k = 0; k < RG_STREAMS && e == cudaSuccess; k++) {
+        e = cudaStreamCreateWithFlags(&p->aux[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->join[k], cudaEventDisableTiming);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
-        if (p->d_sys) cudaFree(p->d_sys);
-        if (p->aux) cudaStreamDestroy(p->aux);
-        if (p->fork) cudaEventDestroy(p->fork);
-        if (p->join) cudaEventDestroy(p->join);
-        delete p;
+        gbla_ragged_plan_destroy(p);
         return from_cuda(e);
     }
     *plan = p;
@@ -339,13 +479,42 @@ GBLA_API gbla_status gbla_ragged_plan_create(const int64_t *a_offsets, const int
 GBLA_API gbla_status gbla_ragged_plan_destroy(gbla_ragged_plan *p) {
     if (!p) return GBLA_SUCCESS;
     cudaError_t e = cudaSuccess;
-    if (p->aux) e = cudaStreamSynchronize(p->aux);
+    for (int k = 0; k < RG_STREAMS; k++)
+        if (p->aux[k]) {
+            cudaError_t e2 = cudaStreamSynchronize(p->aux[k]);
+            if (e == cudaSuccess) e = e2;
+        }
     if (p->d_sys) cudaFree(p->d_sys);
-    if (p->aux) cudaStreamDestroy(p->aux);
+    for (int k = 0; k < RG_STREAMS; k++) {
+        if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
+        if (p->join[k]) cudaEventDestroy(p->join[k]);
+    }
     if (p->fork) cudaEventDestroy(p->fork);
-    if (p->join) cudaEventDestroy(p->join);
     delete p;
     return from_cuda(e);
+}
+
+GBLA_API gbla_status gbla_ragged_plan_get_config(const gbla_ragged_plan *p, gbla_ragged_config *cfg) {
+    if (!p || !cfg) return GBLA_INVALID_VALUE;
+    *cfg = p->cfg;
+    return GBLA_SUCCESS;
+}
+
+GBLA_API gbla_status gbla_ragged_plan_set_config(gbla_ragged_plan *p, const gbla_ragged_config *cfg) {
+    if (!p || !cfg || !config_valid(*cfg)) return GBLA_INVALID_VALUE;
+    p->cfg = *cfg;
+    ragged_buckets(p);
+    return GBLA_SUCCESS;
+}
+
+GBLA_API gbla_status gbla_sragged_autotune(gbla_ragged_plan *p, const float *A, const float *B, int refine_iters,
+                                           int reps, gbla_ragged_config *best, float *best_ms, cudaStream_t st) {
+    return ragged_autotune<float>(p, A, B, refine_iters, reps, best, best_ms, st);
+}
+
+GBLA_API gbla_status gbla_dragged_autotune(gbla_ragged_plan *p, const double *A, const double *B, int refine_iters,
+                                           int reps, gbla_ragged_config *best, float *best_ms, cudaStream_t st) {
+    return ragged_autotune<double>(p, A, B, refine_iters, reps, best, best_ms, st);
 }
 
 GBLA_API gbla_status gbla_sposv_ragged(const gbla_ragged_plan *plan, float *A, float *B, int *info, int refine_iters,

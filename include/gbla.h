@@ -107,8 +107,8 @@ gbla_status gbla_dposv_batched(int n, int nrhs, double *A, int64_t strideA, doub
  * n_i x n_i matrix at A + a_offsets[i] and its n_i x nrhs_i right-hand sides
  * at B + b_offsets[i] (element offsets, column-major, 1 <= n_i <= 128).
  * The plan sorts the systems into size classes (largest first) once; it owns
- * a small device table, an auxiliary stream and two events, so create it at
- * set-up time (it allocates and synchronises) and do not use one plan from
+ * a small device table, three auxiliary streams and four events, so create it
+ * at set-up time (it allocates and synchronises) and do not use one plan from
  * two host threads at once.  No reference counterpart: GPUtils needs one
  * CholeskyBatchFactoriser per size and one potrs per column
  * (include/tensor.cuh:2100-2197). */
@@ -116,6 +116,31 @@ typedef struct gbla_ragged_plan gbla_ragged_plan;
 gbla_status gbla_ragged_plan_create(const int64_t *a_offsets, const int64_t *b_offsets, const int *n,
                                     const int *nrhs, int count, gbla_ragged_plan **plan);
 gbla_status gbla_ragged_plan_destroy(gbla_ragged_plan *plan);
+
+/* Launch configuration of a plan.  Systems with n <= 32 run the lane-row
+ * kernel (8, 16 or 32 lanes per system); the n > 32 systems run one block per
+ * system, cut into buckets of width bucket_width in n (96: one bucket; 48, 32,
+ * 16: more launches, each sized for its own largest system), with
+ * large_threads threads per block (128, 256, 512); fork_small puts the small
+ * classes on their own forked stream.  Default {96, 256, 1}.  The result of a
+ * call does not depend on the configuration (bit-identical). */
+typedef struct gbla_ragged_config {
+    int bucket_width;
+    int large_threads;
+    int fork_small;
+} gbla_ragged_config;
+gbla_status gbla_ragged_plan_get_config(const gbla_ragged_plan *plan, gbla_ragged_config *config);
+gbla_status gbla_ragged_plan_set_config(gbla_ragged_plan *plan, const gbla_ragged_config *config);
+
+/* Autotuner: times every configuration (4 bucket widths x 3 block sizes x 2
+ * stream layouts) on this batch -- best of `reps` runs after a warm-up, each
+ * on fresh copies of A and B -- and keeps the fastest in the plan.  A and B
+ * are not modified.  best / best_ms (nullable) receive the choice and its
+ * time.  Allocates scratch copies and synchronises: a set-up call. */
+gbla_status gbla_sragged_autotune(gbla_ragged_plan *plan, const float *A, const float *B, int refine_iters,
+                                  int reps, gbla_ragged_config *best, float *best_ms, cudaStream_t stream);
+gbla_status gbla_dragged_autotune(gbla_ragged_plan *plan, const double *A, const double *B, int refine_iters,
+                                  int reps, gbla_ragged_config *best, float *best_ms, cudaStream_t stream);
 
 /* Factor + solve every system of the plan (device on which the plan was
  * created; stream-ordered; graph-capturable).  A_i receives its FP32 Cholesky

@@ -96,6 +96,7 @@ def test_invalid_plans(gbla_lib, cuda):
     st, p = _plan(gbla_lib, [], [], [], [])
     assert st == 0
     assert gbla_lib.gbla_sposv_ragged(p, None, None, None, 1, stream()) == 0   # empty plan: no-op
+    assert gbla_lib.gbla_sragged_autotune(p, None, None, 1, 1, None, None, stream()) == 0
     assert gbla_lib.gbla_ragged_plan_destroy(p) == 0
 
 
@@ -123,3 +124,61 @@ def test_d3_config_full_size(gbla_lib, cuda, dt):
         x = X[b_off[i]:b_off[i] + k * r].reshape(r, k).T.astype(np.float64)
         worst = max(worst, np.linalg.norm(M @ x - b) / np.linalg.norm(b))
     assert worst < 1e-6
+
+
+class Cfg(C.Structure):
+    _fields_ = [("bucket_width", C.c_int), ("large_threads", C.c_int), ("fork_small", C.c_int)]
+
+
+def test_config_get_set_and_invalid(gbla_lib, cuda):
+    n, nrhs, a_off, b_off, A, B = workloads.d3_ragged(count=200, seed=3, dtype=np.float64)
+    st, p = _plan(gbla_lib, a_off, b_off, n, nrhs)
+    assert st == 0
+    c = Cfg()
+    assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(c)) == 0
+    assert (c.bucket_width, c.large_threads, c.fork_small) == (96, 256, 1)
+    for bad in (Cfg(17, 256, 1), Cfg(32, 64, 1), Cfg(32, 256, 2)):
+        assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(bad)) == 1
+    assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(Cfg(16, 512, 0))) == 0
+    assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(c)) == 0
+    assert (c.bucket_width, c.large_threads, c.fork_small) == (16, 512, 0)
+    assert gbla_lib.gbla_ragged_plan_destroy(p) == 0
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_every_configuration_gives_identical_results_and_autotune_keeps_inputs(gbla_lib, cuda, dt):
+    import torch
+    n, nrhs, a_off, b_off, A, B = workloads.d3_ragged(count=3000, seed=8, dtype=np.float64)
+    st, p = _plan(gbla_lib, a_off, b_off, n, nrhs)
+    assert st == 0
+    Ah, Bh = torch.tensor(A.astype(dt)).cuda(), torch.tensor(B.astype(dt)).cuda()
+    fn = gbla_lib.gbla_sposv_ragged if dt == np.float32 else gbla_lib.gbla_dposv_ragged
+    tune = gbla_lib.gbla_sragged_autotune if dt == np.float32 else gbla_lib.gbla_dragged_autotune
+    refine = 1 if dt == np.float32 else 2
+
+    def run():
+        Ad, Bd = Ah.clone(), Bh.clone()
+        info = torch.full((len(n),), -1, dtype=torch.int32, device="cuda")
+        assert fn(p, Ad.data_ptr(), Bd.data_ptr(), info.data_ptr(), refine, stream()) == 0
+        torch.cuda.synchronize()
+        assert (info == 0).all()
+        return Ad, Bd
+
+    A0, X0 = run()
+    for cfg in (Cfg(48, 128, 0), Cfg(32, 512, 1), Cfg(16, 256, 1)):
+        assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(cfg)) == 0
+        A1, X1 = run()
+        assert torch.equal(A1, A0) and torch.equal(X1, X0)
+    Ak, Bk = Ah.clone(), Bh.clone()
+    best, ms = Cfg(), C.c_float()
+    assert tune(p, Ak.data_ptr(), Bk.data_ptr(), refine, 2, C.byref(best), C.byref(ms), stream()) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(Ak, Ah) and torch.equal(Bk, Bh)       # inputs untouched
+    assert best.bucket_width in (96, 48, 32, 16) and best.large_threads in (128, 256, 512) and ms.value > 0
+    cur = Cfg()
+    assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(cur)) == 0
+    assert (cur.bucket_width, cur.large_threads, cur.fork_small) == (best.bucket_width, best.large_threads,
+                                                                   best.fork_small)
+    A2, X2 = run()
+    assert torch.equal(A2, A0) and torch.equal(X2, X0)
+    assert gbla_lib.gbla_ragged_plan_destroy(p) == 0
