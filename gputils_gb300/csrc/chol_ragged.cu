@@ -138,12 +138,58 @@ __global__ void __launch_bounds__(128, 1)
 template <typename T>
 __host__ __device__ inline size_t ragged_large_smem(int nmax, int warps) {
     const int ld = cta_ld(nmax);
-    // float factor (n x ld) + float dinv (n) + float work (warps x n) + T x (warps x n)
-    return sizeof(float) * ((size_t)nmax * ld + nmax + (size_t)warps * nmax) + sizeof(T) * (size_t)warps * nmax + 64;
+    // panel rows (n x 8, 16-byte aligned) + float factor (n x ld) + float dinv (n, padded to
+    // an even count so that x stays 8-byte aligned) + T x (warps x n)
+    return sizeof(float) * ((size_t)nmax * 8 + (size_t)nmax * ld + (size_t)round_up(nmax, 2)) +
+           sizeof(T) * (size_t)warps * nmax + 64;
 }
 
+// Solve L L^T x = b for one column held in registers (element lane + 32 t in
+// x[t], n <= 128): the pivot value travels by shuffle, L is read from shared
+// memory (column-major, odd stride, so row and column walks are both
+// conflict-free).  The step loop runs over (register chunk tk, lane lk) with
+// tk known at compile time, so the pivot register needs no select and only
+// the pivot's own chunk needs a row comparison.  Per element the updates run
+// in the same order as a column-oriented shared-memory solve.
+__device__ __forceinline__ void reg_solve(const float *__restrict__ a, int ld, const float *__restrict__ dinv,
+                                          float (&x)[4], int n, int lane) {
+    const int nt = (n + 31) >> 5;
+#pragma unroll
+    for (int tk = 0; tk < 4; tk++) {
+        if (tk >= nt) break;
+        const int kmax = n - 32 * tk < 32 ? n - 32 * tk : 32;
+        for (int lk = 0; lk < kmax; lk++) {
+            const int k = 32 * tk + lk;
+            const float yk = shfl(x[tk], lk) * dinv[k];
+            if (lane == lk) x[tk] = yk;
+            const float *col = a + k * ld + lane;
+            if (lane > lk) x[tk] = fmaf(-col[32 * tk], yk, x[tk]);
+#pragma unroll
+            for (int t = tk + 1; t < 4; t++)
+                if (t < nt) x[t] = fmaf(-col[32 * t], yk, x[t]);
+        }
+    }
+#pragma unroll
+    for (int tk = 3; tk >= 0; tk--) {
+        if (tk >= nt) continue;
+        const int kmax = n - 32 * tk < 32 ? n - 32 * tk : 32;
+        for (int lk = kmax - 1; lk >= 0; lk--) {
+            const int k = 32 * tk + lk;
+            const float zk = shfl(x[tk], lk) * dinv[k];
+            if (lane == lk) x[tk] = zk;
+            const float *row = a + lane * ld + k;  // L(k, i) for i = lane + 32 t
+            if (lane < lk) x[tk] = fmaf(-row[32 * tk * ld], zk, x[tk]);
+#pragma unroll
+            for (int t = 0; t < tk; t++) x[t] = fmaf(-row[32 * t * ld], zk, x[t]);
+        }
+    }
+}
+
+constexpr int RG_PANEL = 8;
+
+// at least 3 blocks of 256 (6 of 128, 12 of 64, 1 of 512) per SM: register cap ~85
 template <typename T, int THREADS>
-__global__ void __launch_bounds__(THREADS)
+__global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
     k_ragged_large(const RaggedSys *__restrict__ sys, int first, int nmax, const T *__restrict__ A_in,
                    T *__restrict__ A, T *__restrict__ B, int *__restrict__ info, int refine) {
     constexpr int RG_LARGE_WARPS = THREADS / 32;
@@ -151,10 +197,10 @@ __global__ void __launch_bounds__(THREADS)
     const RaggedSys s = sys[first + blockIdx.x];
     const int n = s.n, nrhs = s.nrhs, ld = cta_ld(n);
     const int ldmax = cta_ld(nmax);
-    float *a = reinterpret_cast<float *>(rsm);
+    float *prow = reinterpret_cast<float *>(rsm);  // panel row r at prow[8 r .. 8 r + 7]
+    float *a = prow + (size_t)nmax * 8;
     float *dinv = a + (size_t)nmax * ldmax;
-    float *work = dinv + nmax;
-    T *xs = reinterpret_cast<T *>(work + (size_t)RG_LARGE_WARPS * nmax);
+    T *xs = reinterpret_cast<T *>(dinv + round_up(nmax, 2) + ((nmax * 8 + (size_t)nmax * ldmax) & 1));
     __shared__ int s_fail;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const T *ag = A_in + s.a_off;
@@ -163,38 +209,108 @@ __global__ void __launch_bounds__(THREADS)
         for (int i = j + lane; i < n; i += 32) a[(int64_t)j * ld + i] = (float)ag[(int64_t)j * n + i];
     if (threadIdx.x == 0) s_fail = 0;
     __syncthreads();
-    // right-looking factorisation, one barrier per column (as in the uniform kernel)
-    for (int k = 0; k < n; k++) {
-        if (warp == k % RG_LARGE_WARPS) {
-            __syncwarp();
-            const float d = a[(int64_t)k * ld + k];
-            if (!(d > 0.f) && lane == 0 && s_fail == 0) s_fail = k + 1;
-            const float l = sqrtf(d), il = 1.f / l;
-            for (int i = k + 1 + lane; i < n; i += 32) a[(int64_t)k * ld + i] *= il;
-            if (lane == 0) { a[(int64_t)k * ld + k] = l; dinv[k] = il; }
+    // Blocked right-looking factorisation: warp 0 factors a panel of 8
+    // columns in registers (rows k0 + lane + 32 t), then every warp applies
+    // the panel's rank-8 update to the trailing lower triangle.  Each
+    // element receives its updates in increasing k with one fma each, as in
+    // the column-by-column algorithm.  Two barriers per panel.
+    for (int k0 = 0; k0 < n; k0 += RG_PANEL) {
+        const int pw = n - k0 < RG_PANEL ? n - k0 : RG_PANEL;
+        if (warp == 0) {
+            float pv[4][RG_PANEL];
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+#pragma unroll
+                for (int c = 0; c < RG_PANEL; c++) {
+                    const int r = k0 + lane + 32 * t;
+                    pv[t][c] = (c < pw && r < n) ? a[(int64_t)(k0 + c) * ld + r] : 0.f;
+                }
+#pragma unroll
+            for (int c = 0; c < RG_PANEL; c++) {
+                if (c >= pw) break;
+                const int k = k0 + c;
+                const float d = shfl(pv[0][c], c);  // row k sits in lane c, t = 0
+                if (!(d > 0.f) && lane == 0 && s_fail == 0) s_fail = k + 1;
+                const float l = sqrtf(d), il = 1.f / l;
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const int r = k0 + lane + 32 * t;
+                    if (r > k) pv[t][c] *= il;
+                }
+                if (lane == c) pv[0][c] = l;
+                if (lane == 0) dinv[k] = il;
+#pragma unroll
+                for (int c2 = c + 1; c2 < RG_PANEL; c2++) {
+                    if (c2 >= pw) break;
+                    const float ljk = shfl(pv[0][c], c2);  // L(k0 + c2, k)
+#pragma unroll
+                    for (int t = 0; t < 4; t++) {
+                        const int r = k0 + lane + 32 * t;
+                        if (r >= k0 + c2) pv[t][c2] = fmaf(-pv[t][c], ljk, pv[t][c2]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int r = k0 + lane + 32 * t;
+                if (r >= n) continue;
+#pragma unroll
+                for (int c = 0; c < RG_PANEL; c++)
+                    if (c < pw && r >= k0 + c) a[(k0 + c) * ld + r] = pv[t][c];
+                // the panel's rows for the trailing update, row-major (zero past pw)
+                float4 *pr = reinterpret_cast<float4 *>(prow + 8 * r);
+                pr[0] = make_float4(pv[t][0], pw > 1 ? pv[t][1] : 0.f, pw > 2 ? pv[t][2] : 0.f,
+                                    pw > 3 ? pv[t][3] : 0.f);
+                pr[1] = make_float4(pw > 4 ? pv[t][4] : 0.f, pw > 5 ? pv[t][5] : 0.f, pw > 6 ? pv[t][6] : 0.f,
+                                    pw > 7 ? pv[t][7] : 0.f);
+            }
         }
         __syncthreads();
-        const int j0 = k + 1 + ((warp - (k + 1) % RG_LARGE_WARPS) + RG_LARGE_WARPS) % RG_LARGE_WARPS;
-        for (int j = j0; j < n; j += RG_LARGE_WARPS) {
-            const float ljk = a[(int64_t)k * ld + j];
-            for (int i = j + lane; i < n; i += 32) a[(int64_t)j * ld + i] -= a[(int64_t)k * ld + i] * ljk;
+        const int kend = k0 + pw;
+        for (int j = kend + warp; j < n; j += RG_LARGE_WARPS) {
+            const float4 lj0 = reinterpret_cast<const float4 *>(prow + 8 * j)[0];
+            const float4 lj1 = reinterpret_cast<const float4 *>(prow + 8 * j)[1];
+            float *colj = a + j * ld;
+            for (int i = j + lane; i < n; i += 32) {
+                const float4 li0 = reinterpret_cast<const float4 *>(prow + 8 * i)[0];
+                const float4 li1 = reinterpret_cast<const float4 *>(prow + 8 * i)[1];
+                float acc = colj[i];
+                // increasing k, one fma each (zeros past pw leave acc unchanged)
+                acc = fmaf(-li0.x, lj0.x, acc);
+                acc = fmaf(-li0.y, lj0.y, acc);
+                acc = fmaf(-li0.z, lj0.z, acc);
+                acc = fmaf(-li0.w, lj0.w, acc);
+                acc = fmaf(-li1.x, lj1.x, acc);
+                acc = fmaf(-li1.y, lj1.y, acc);
+                acc = fmaf(-li1.z, lj1.z, acc);
+                acc = fmaf(-li1.w, lj1.w, acc);
+                colj[i] = acc;
+            }
         }
+        __syncthreads();
     }
-    __syncthreads();
     if (threadIdx.x == 0 && info) info[s.orig] = s_fail;
 
     T *bg = B + s.b_off;
-    float *w = work + (size_t)warp * nmax;
     T *x = xs + (size_t)warp * nmax;
     for (int c = warp; c < nrhs; c += RG_LARGE_WARPS) {
         const T *bc = bg + (int64_t)c * n;
-        for (int i = lane; i < n; i += 32) w[i] = (float)bc[i];
-        __syncwarp();
-        cta_solve_col<float>(a, ld, dinv, w, n, lane);
-        for (int i = lane; i < n; i += 32) x[i] = (T)w[i];
+        float w[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int i = lane + 32 * t;
+            w[t] = i < n ? (float)bc[i] : 0.f;
+        }
+        reg_solve(a, ld, dinv, w, n, lane);
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int i = lane + 32 * t;
+            if (i < n) x[i] = (T)w[t];
+        }
         __syncwarp();
         for (int it = 0; it < refine; it++) {
-            // r = b - A x with the full symmetric A; rows lane + 32 t
+            // r = b - A x with the full symmetric A; rows lane + 32 t; the
+            // columns of A are loaded four at a time to keep loads in flight
             if constexpr (sizeof(T) == 4) {
                 ff acc[4];
 #pragma unroll
@@ -203,7 +319,26 @@ __global__ void __launch_bounds__(THREADS)
                     acc[t].h = i < n ? (float)bc[i] : 0.f;
                     acc[t].l = 0.f;
                 }
-                for (int j = 0; j < n; j++) {
+                const int nt = (n + 31) >> 5;
+                int j = 0;
+                for (; j + 4 <= n; j += 4) {
+                    float av[4][4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+#pragma unroll
+                        for (int t = 0; t < 4; t++) {
+                            const int i = lane + 32 * t;
+                            av[q][t] = (t < nt && i < n) ? (float)ag[(int64_t)(j + q) * n + i] : 0.f;
+                        }
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const float xj = (float)x[j + q];
+#pragma unroll
+                        for (int t = 0; t < 4; t++)
+                            if (t < nt) ff_fma(acc[t], -av[q][t], xj, 0.f);
+                    }
+                }
+                for (; j < n; j++) {
                     const float xj = (float)x[j];
 #pragma unroll
                     for (int t = 0; t < 4; t++) {
@@ -211,12 +346,8 @@ __global__ void __launch_bounds__(THREADS)
                         if (i < n) ff_fma(acc[t], -(float)ag[(int64_t)j * n + i], xj, 0.f);
                     }
                 }
-                __syncwarp();
 #pragma unroll
-                for (int t = 0; t < 4; t++) {
-                    const int i = lane + 32 * t;
-                    if (i < n) w[i] = acc[t].h + acc[t].l;
-                }
+                for (int t = 0; t < 4; t++) w[t] = acc[t].h + acc[t].l;
             } else {
                 double acc[4];
 #pragma unroll
@@ -224,7 +355,26 @@ __global__ void __launch_bounds__(THREADS)
                     const int i = lane + 32 * t;
                     acc[t] = i < n ? (double)bc[i] : 0.0;
                 }
-                for (int j = 0; j < n; j++) {
+                const int nt = (n + 31) >> 5;
+                int j = 0;
+                for (; j + 4 <= n; j += 4) {
+                    double av[4][4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+#pragma unroll
+                        for (int t = 0; t < 4; t++) {
+                            const int i = lane + 32 * t;
+                            av[q][t] = (t < nt && i < n) ? (double)ag[(int64_t)(j + q) * n + i] : 0.0;
+                        }
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const double xj = (double)x[j + q];
+#pragma unroll
+                        for (int t = 0; t < 4; t++)
+                            if (t < nt) acc[t] = fma(-av[q][t], xj, acc[t]);
+                    }
+                }
+                for (; j < n; j++) {
                     const double xj = (double)x[j];
 #pragma unroll
                     for (int t = 0; t < 4; t++) {
@@ -232,16 +382,16 @@ __global__ void __launch_bounds__(THREADS)
                         if (i < n) acc[t] = fma(-(double)ag[(int64_t)j * n + i], xj, acc[t]);
                     }
                 }
-                __syncwarp();
 #pragma unroll
-                for (int t = 0; t < 4; t++) {
-                    const int i = lane + 32 * t;
-                    if (i < n) w[i] = (float)acc[t];
-                }
+                for (int t = 0; t < 4; t++) w[t] = (float)acc[t];
             }
+            reg_solve(a, ld, dinv, w, n, lane);
             __syncwarp();
-            cta_solve_col<float>(a, ld, dinv, w, n, lane);
-            for (int i = lane; i < n; i += 32) x[i] = x[i] + (T)w[i];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int i = lane + 32 * t;
+                if (i < n) x[i] = x[i] + (T)w[t];
+            }
             __syncwarp();
         }
         T *bo = bg + (int64_t)c * n;
@@ -317,7 +467,8 @@ static gbla_status ragged_launch(const gbla_ragged_plan *p, T *A, T *B, int *inf
         const int sidx = large_streams > 0 ? b % large_streams : 0;
         cudaStream_t ls = sidx == 0 ? st : p->aux[sidx];
         gbla_status s;
-        if (p->cfg.large_threads == 128) s = launch_large<T, 128>(p, b, A, B, info, refine, ls);
+        if (p->cfg.large_threads == 64) s = launch_large<T, 64>(p, b, A, B, info, refine, ls);
+        else if (p->cfg.large_threads == 128) s = launch_large<T, 128>(p, b, A, B, info, refine, ls);
         else if (p->cfg.large_threads == 512) s = launch_large<T, 512>(p, b, A, B, info, refine, ls);
         else s = launch_large<T, 256>(p, b, A, B, info, refine, ls);
         if (s != GBLA_SUCCESS) return s;
@@ -346,7 +497,7 @@ static gbla_status ragged_launch(const gbla_ragged_plan *p, T *A, T *B, int *inf
 
 static bool config_valid(const gbla_ragged_config &c) {
     return (c.bucket_width == 16 || c.bucket_width == 32 || c.bucket_width == 48 || c.bucket_width == 96) &&
-           (c.large_threads == 128 || c.large_threads == 256 || c.large_threads == 512) &&
+           (c.large_threads == 64 || c.large_threads == 128 || c.large_threads == 256 || c.large_threads == 512) &&
            (c.fork_small == 0 || c.fork_small == 1);
 }
 
@@ -381,9 +532,9 @@ static gbla_status ragged_autotune(gbla_ragged_plan *p, const T *A, const T *B, 
     const gbla_ragged_config saved = p->cfg;
     gbla_ragged_config best = saved;
     float best_t = 3.4e38f;
-    const int widths[4] = {96, 48, 32, 16}, threads[3] = {128, 256, 512};
+    const int widths[4] = {96, 48, 32, 16}, threads[4] = {64, 128, 256, 512};
     for (int wi = 0; wi < 4 && status == GBLA_SUCCESS; wi++)
-        for (int ti = 0; ti < 3 && status == GBLA_SUCCESS; ti++)
+        for (int ti = 0; ti < 4 && status == GBLA_SUCCESS; ti++)
             for (int f = 0; f < 2 && status == GBLA_SUCCESS; f++) {
                 p->cfg = {widths[wi], threads[ti], f};
                 ragged_buckets(p);

@@ -121,7 +121,7 @@ gbla_status gbla_ragged_plan_destroy(gbla_ragged_plan *plan);
  * kernel (8, 16 or 32 lanes per system); the n > 32 systems run one block per
  * system, cut into buckets of width bucket_width in n (96: one bucket; 48, 32,
  * 16: more launches, each sized for its own largest system), with
- * large_threads threads per block (128, 256, 512); fork_small puts the small
+ * large_threads threads per block (64, 128, 256, 512); fork_small puts the small
  * classes on their own forked stream.  Default {96, 256, 1}.  The result of a
  * call does not depend on the configuration (bit-identical). */
 typedef struct gbla_ragged_config {
@@ -132,7 +132,7 @@ typedef struct gbla_ragged_config {
 gbla_status gbla_ragged_plan_get_config(const gbla_ragged_plan *plan, gbla_ragged_config *config);
 gbla_status gbla_ragged_plan_set_config(gbla_ragged_plan *plan, const gbla_ragged_config *config);
 
-/* Autotuner: times every configuration (4 bucket widths x 3 block sizes x 2
+/* Autotuner: times every configuration (4 bucket widths x 4 block sizes x 2
  * stream layouts) on this batch -- best of `reps` runs after a warm-up, each
  * on fresh copies of A and B -- and keeps the fastest in the plan.  A and B
  * are not modified.  best / best_ms (nullable) receive the choice and its

@@ -137,7 +137,7 @@ def test_config_get_set_and_invalid(gbla_lib, cuda):
     c = Cfg()
     assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(c)) == 0
     assert (c.bucket_width, c.large_threads, c.fork_small) == (96, 256, 1)
-    for bad in (Cfg(17, 256, 1), Cfg(32, 64, 1), Cfg(32, 256, 2)):
+    for bad in (Cfg(17, 256, 1), Cfg(32, 96, 1), Cfg(32, 256, 2)):
         assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(bad)) == 1
     assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(Cfg(16, 512, 0))) == 0
     assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(c)) == 0
@@ -165,7 +165,7 @@ def test_every_configuration_gives_identical_results_and_autotune_keeps_inputs(g
         return Ad, Bd
 
     A0, X0 = run()
-    for cfg in (Cfg(48, 128, 0), Cfg(32, 512, 1), Cfg(16, 256, 1)):
+    for cfg in (Cfg(48, 128, 0), Cfg(32, 512, 1), Cfg(16, 256, 1), Cfg(16, 64, 1)):
         assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(cfg)) == 0
         A1, X1 = run()
         assert torch.equal(A1, A0) and torch.equal(X1, X0)
@@ -174,7 +174,7 @@ def test_every_configuration_gives_identical_results_and_autotune_keeps_inputs(g
     assert tune(p, Ak.data_ptr(), Bk.data_ptr(), refine, 2, C.byref(best), C.byref(ms), stream()) == 0
     torch.cuda.synchronize()
     assert torch.equal(Ak, Ah) and torch.equal(Bk, Bh)       # inputs untouched
-    assert best.bucket_width in (96, 48, 32, 16) and best.large_threads in (128, 256, 512) and ms.value > 0
+    assert best.bucket_width in (96, 48, 32, 16) and best.large_threads in (64, 128, 256, 512) and ms.value > 0
     cur = Cfg()
     assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(cur)) == 0
     assert (cur.bucket_width, cur.large_threads, cur.fork_small) == (best.bucket_width, best.large_threads,
