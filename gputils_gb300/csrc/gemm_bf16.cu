@@ -103,7 +103,9 @@ __global__ void __launch_bounds__(BG_THREADS, 2)
     __shared__ uint32_t s_tmem;
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.x * BG_BM, n0 = blockIdx.y * BG_BN;
+    // N tiles vary fastest: the CTAs that share an A row panel run together and
+    // read it once from DRAM (through L2)
+    const int m0 = blockIdx.y * BG_BM, n0 = blockIdx.x * BG_BN;
     const int KT = (K + BG_BK - 1) / BG_BK;
 
     if (tid == 0) {
@@ -319,7 +321,7 @@ gbla_status gemm_bf16_tn(int M, int N, int K, const void *A, int64_t lda, const 
         if (e != cudaSuccess) return from_cuda(e);
         attr_done[dev] = true;
     }
-    dim3 grid((unsigned)((M + BG_BM - 1) / BG_BM), (unsigned)((N + BG_BN - 1) / BG_BN));
+    dim3 grid((unsigned)((N + BG_BN - 1) / BG_BN), (unsigned)((M + BG_BM - 1) / BG_BM));
     if (grid.y > 65535) return GBLA_INVALID_VALUE;
     k_gemm_bf16_tn<<<grid, BG_THREADS, BG_SMEM, st>>>(ma, mb, M, N, K, epi);
     return launch_status();

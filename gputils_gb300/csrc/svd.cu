@@ -110,7 +110,9 @@ __device__ __forceinline__ bool jacobi_rotation_t<double>(double alpha, double b
 }
 
 // ----------------------------------------------------------- warp kernel
-template <typename T, int MR>
+// BUDGET: warm start with a sweep budget and cold restart (gbla_sgesvj_warm_batched);
+// a separate instantiation, so the plain path keeps its register footprint.
+template <typename T, int MR, bool BUDGET>
 __global__ void __launch_bounds__(128, 1)
     k_gesvj_warp(int m, int n, const T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
                  T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(128, 1)
     tol = jacobi_tol<T>(tol, m);
 
     // warm start with a sweep budget: past it, restart cold from A (V = I)
-    const bool budgeted = V0 && warm_budget > 0;
+    const bool budgeted = BUDGET && V0 && warm_budget > 0;
     int sweep = 0, total = 0, converged = 0, restarted = 0;
     int limit = budgeted ? warm_budget : max_sweeps;
     for (;;) {
@@ -195,12 +197,14 @@ __global__ void __launch_bounds__(128, 1)
         if (!__any_sync(FULL, rotated)) { converged = 1; break; }
     }
     if (converged || restarted || !budgeted) break;
+    if constexpr (BUDGET) {
 #pragma unroll
-    for (int i = 0; i < MR; i++) a[i] = (col && i < m) ? ag[(int64_t)lane * m + i] : 0.f;
+        for (int i = 0; i < MR; i++) a[i] = (col && i < m) ? ag[(int64_t)lane * m + i] : 0.f;
 #pragma unroll
-    for (int i = 0; i < 32; i++) v[i] = (col && i == lane) ? 1.f : 0.f;
-    restarted = 1;
-    limit = max_sweeps;
+        for (int i = 0; i < 32; i++) v[i] = (col && i == lane) ? 1.f : 0.f;
+        restarted = 1;
+        limit = max_sweeps;
+    }
     }
 
     // ---- epilogue.  The rotated columns' norms drift by ~sqrt(#rotations) ulp;
@@ -306,7 +310,11 @@ __global__ void __launch_bounds__(128, 1)
 constexpr int SVJ_CTA_THREADS = 256;
 constexpr int SVJ_GROUP = 8;
 
-template <typename T>
+// MR, NR: row counts of A and V padded to 32, 64 or 128 (compile time).  The
+// padding rows hold zeros, which every rotation maps to zeros, so the row
+// loops need no bounds tests and unroll completely; a lane walks rows
+// (gl + rot + 8 t) mod MR.
+template <typename T, int MR, int NR>
 __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
     k_gesvj_cta(int m, int n, const T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
                 T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
@@ -314,7 +322,7 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
                 int *__restrict__ info, int *__restrict__ sweeps_out, int batch) {
     extern __shared__ __align__(16) unsigned char svsm_raw[];
     T *svsm = reinterpret_cast<T *>(svsm_raw);
-    const int lda = (int)round_up(m, 32), ldv = (int)round_up(n, 32);
+    constexpr int lda = MR, ldv = NR;
     T *a = svsm;                      // n columns x lda
     T *v = a + (size_t)n * lda;       // n columns x ldv
     T *sig = v + (size_t)n * ldv;     // n
@@ -322,17 +330,19 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
     T *nrm = rinv + n;                // n: cached |a_j|^2
     const int tid = threadIdx.x, g = tid / SVJ_GROUP, gl = tid % SVJ_GROUP;
     const int N = n + (n & 1), M = N - 1;
-    // row walk of this lane: rows (gl + rot + 8 t) mod mr, t < mr / 8
     const int rot = 8 * (g & 3);
-    const int mr = (int)round_up(m, 8), nr = (int)round_up(n, 8);
-    const int ma0 = (gl + rot) % mr, va0 = (gl + rot) % nr;
+    const int w0 = gl + rot;  // < 32 <= MR, NR
+    constexpr int MT = MR / 8, NT = NR / 8;
 
     for (int64_t mat = blockIdx.x; mat < batch; mat += gridDim.x) {
         const T *ag = A + mat * sA;
-        for (int e = tid; e < m * n; e += SVJ_CTA_THREADS) a[(e / m) * lda + e % m] = ag[e];
-        for (int e = tid; e < n * n; e += SVJ_CTA_THREADS) {
-            int i = e % n, j = e / n;
-            v[j * ldv + i] = V0 ? V0[mat * sV0 + e] : (i == j ? 1.f : 0.f);
+        for (int e = tid; e < MR * n; e += SVJ_CTA_THREADS) {
+            const int i = e % MR, j = e / MR;
+            a[j * lda + i] = i < m ? ag[(int64_t)j * m + i] : T(0);
+        }
+        for (int e = tid; e < NR * n; e += SVJ_CTA_THREADS) {
+            const int i = e % NR, j = e / NR;
+            v[j * ldv + i] = i >= n ? T(0) : V0 ? V0[mat * sV0 + (int64_t)j * n + i] : (i == j ? T(1) : T(0));
         }
         __syncthreads();
         if (V0) {
@@ -385,9 +395,14 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
             for (int j0 = 0; j0 < n; j0 += SVJ_CTA_THREADS / SVJ_GROUP) {
                 const int j = j0 + g;
                 T f = 0.f;
-                if (j < n)
-                    for (int t = 0, i = ma0; t < mr / 8; t++, i = (i + 8 < mr) ? i + 8 : i + 8 - mr)
-                        if (i < m) f = fma(a[j * lda + i], a[j * lda + i], f);
+                if (j < n) {
+                    const T *col = a + j * lda;
+#pragma unroll
+                    for (int t = 0; t < MT; t++) {
+                        const T x = col[(w0 + 8 * t) & (MR - 1)];
+                        f = fma(x, x, f);
+                    }
+                }
                 f = group_sum(f, SVJ_GROUP);
                 if (gl == 0 && j < n) nrm[j] = f;
             }
@@ -410,9 +425,13 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
                 }
                 const bool act = q >= 0 && q < n;
                 T gamma = 0.f, alpha = 0.f, beta = 0.f;
+                T *ap = a + (act ? p : 0) * lda, *aq = a + (act ? q : 0) * lda;
                 if (act) {
-                    for (int t = 0, i = ma0; t < mr / 8; t++, i = (i + 8 < mr) ? i + 8 : i + 8 - mr)
-                        if (i < m) gamma = fma(a[p * lda + i], a[q * lda + i], gamma);
+#pragma unroll
+                    for (int t = 0; t < MT; t++) {
+                        const int i = (w0 + 8 * t) & (MR - 1);
+                        gamma = fma(ap[i], aq[i], gamma);
+                    }
                     alpha = nrm[p];
                     beta = nrm[q];
                 }
@@ -420,17 +439,20 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
                 T c, sn, tn;
                 if (act && jacobi_rotation_t<T>(alpha, beta, gamma, tol_eff, small, c, sn, tn)) {
                     rotated = 1;
-                    for (int t = 0, i = ma0; t < mr / 8; t++, i = (i + 8 < mr) ? i + 8 : i + 8 - mr) {
-                        if (i >= m) continue;
-                        T x = a[p * lda + i], y = a[q * lda + i];
-                        a[p * lda + i] = fma(c, x, -sn * y);
-                        a[q * lda + i] = fma(sn, x, c * y);
+#pragma unroll
+                    for (int t = 0; t < MT; t++) {
+                        const int i = (w0 + 8 * t) & (MR - 1);
+                        const T x = ap[i], y = aq[i];
+                        ap[i] = fma(c, x, -sn * y);
+                        aq[i] = fma(sn, x, c * y);
                     }
-                    for (int t = 0, i = va0; t < nr / 8; t++, i = (i + 8 < nr) ? i + 8 : i + 8 - nr) {
-                        if (i >= n) continue;
-                        T x = v[p * ldv + i], y = v[q * ldv + i];
-                        v[p * ldv + i] = fma(c, x, -sn * y);
-                        v[q * ldv + i] = fma(sn, x, c * y);
+                    T *vp = v + p * ldv, *vq = v + q * ldv;
+#pragma unroll
+                    for (int t = 0; t < NT; t++) {
+                        const int i = (w0 + 8 * t) & (NR - 1);
+                        const T x = vp[i], y = vq[i];
+                        vp[i] = fma(c, x, -sn * y);
+                        vq[i] = fma(sn, x, c * y);
                     }
                     if (gl == 0) {
                         nrm[p] = fma(-tn, gamma, alpha);
@@ -444,8 +466,14 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
         }
         if (converged || restarted || !budgeted) break;
         // warm budget spent: restart cold from A with V = I
-        for (int e = tid; e < m * n; e += SVJ_CTA_THREADS) a[(e / m) * lda + e % m] = ag[e];
-        for (int e = tid; e < n * n; e += SVJ_CTA_THREADS) v[(e / n) * ldv + e % n] = (e % n == e / n) ? 1.f : 0.f;
+        for (int e = tid; e < MR * n; e += SVJ_CTA_THREADS) {
+            const int i = e % MR, j = e / MR;
+            a[j * lda + i] = i < m ? ag[(int64_t)j * m + i] : T(0);
+        }
+        for (int e = tid; e < NR * n; e += SVJ_CTA_THREADS) {
+            const int i = e % NR, j = e / NR;
+            v[j * ldv + i] = (i == j) ? T(1) : T(0);
+        }
         __syncthreads();
         restarted = 1;
         limit = max_sweeps;
@@ -543,9 +571,30 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
     }
 }
 
+// padded row count of the block kernel: 32, 64 or 128
+static int svj_pad(int r) { return r <= 32 ? 32 : r <= 64 ? 64 : 128; }
+
+template <typename T, int MR, int NR>
+static gbla_status svj_cta_launch(int m, int n, const T *A, int64_t sA, T *S, int64_t sS, T *Vt, int64_t sVt, T *U,
+                                  int64_t sU, const T *V0, int64_t sV0, T tol, int max_sweeps, int warm_budget,
+                                  int *fallback, int *info, int *sweeps, int batch, size_t smem, cudaStream_t st) {
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_gesvj_cta<T, MR, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return from_cuda(e);
+    }
+    int per_sm = (int)((200 * 1024) / (smem + 1024));
+    per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
+    int64_t grid = (int64_t)sm_count() * per_sm;
+    if (grid > batch) grid = batch;
+    k_gesvj_cta<T, MR, NR><<<(unsigned)grid, SVJ_CTA_THREADS, smem, st>>>(
+        m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, warm_budget, fallback, info, sweeps, batch);
+    return launch_status();
+}
+
 template <typename T>
 static size_t svj_cta_smem(int m, int n) {
-    return sizeof(T) * ((size_t)n * round_up(m, 32) + (size_t)n * round_up(n, 32) + 3 * (size_t)n) + 16;
+    return sizeof(T) * ((size_t)n * svj_pad(m) + (size_t)n * svj_pad(n) + 3 * (size_t)n) + 16;
 }
 
 // ---------------------------------------------------------------- rank
@@ -612,29 +661,39 @@ static gbla_status svd_launch(int m, int n, const T *A, int64_t sA, T *S, int64_
     const int warp_m = sizeof(T) == 4 ? 64 : 32;
     if (n <= 32 && m <= warp_m) {
         const unsigned grid = (unsigned)((batch + 3) / 4);
+        const bool budget = V0 && warm_budget > 0;
         if (m <= 32) {
-            k_gesvj_warp<T, 32><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps,
-                                                      warm_budget, fallback, info, sweeps, batch);
+            if (budget)
+                k_gesvj_warp<T, 32, true><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol,
+                                                                max_sweeps, warm_budget, fallback, info, sweeps,
+                                                                batch);
+            else
+                k_gesvj_warp<T, 32, false><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol,
+                                                                 max_sweeps, 0, fallback, info, sweeps, batch);
         } else if constexpr (sizeof(T) == 4) {
-            k_gesvj_warp<T, 64><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps,
-                                                      warm_budget, fallback, info, sweeps, batch);
+            if (budget)
+                k_gesvj_warp<T, 64, true><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol,
+                                                                max_sweeps, warm_budget, fallback, info, sweeps,
+                                                                batch);
+            else
+                k_gesvj_warp<T, 64, false><<<grid, 128, 0, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol,
+                                                                 max_sweeps, 0, fallback, info, sweeps, batch);
         }
         return launch_status();
     }
     if (n <= 64 && m <= 128) {
-        size_t smem = svj_cta_smem<T>(m, n);
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k_gesvj_cta<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return from_cuda(e);
-        }
-        int per_sm = (int)((200 * 1024) / (smem + 1024));
-        per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
-        int64_t grid = (int64_t)sm_count() * per_sm;
-        if (grid > batch) grid = batch;
-        k_gesvj_cta<T><<<(unsigned)grid, SVJ_CTA_THREADS, smem, st>>>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol,
-                                                                    max_sweeps, warm_budget, fallback, info, sweeps,
-                                                                    batch);
-        return launch_status();
+        const size_t smem = svj_cta_smem<T>(m, n);
+        const int mr = svj_pad(m), nr = svj_pad(n);
+#define SVJ_LAUNCH(MRV, NRV)                                                                                      \
+    if (mr == MRV && nr == NRV)                                                                                   \
+        return svj_cta_launch<T, MRV, NRV>(m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps,          \
+                                           warm_budget, fallback, info, sweeps, batch, smem, st);
+        SVJ_LAUNCH(32, 32)
+        SVJ_LAUNCH(64, 32)
+        SVJ_LAUNCH(128, 32)
+        SVJ_LAUNCH(64, 64)
+        SVJ_LAUNCH(128, 64)
+#undef SVJ_LAUNCH
     }
     return GBLA_NOT_SUPPORTED;
 }
