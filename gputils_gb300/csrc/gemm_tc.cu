@@ -106,7 +106,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TC_THREADS, 2)
     k_gemm_tc_bf16x6(float alpha, const float *__restrict__ A, int64_t sA, const float *__restrict__ B, int64_t sB,
                      float beta, float *__restrict__ C, int64_t sC, int batch) {
     extern __shared__ __align__(1024) unsigned char smem[];
