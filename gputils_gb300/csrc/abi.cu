@@ -24,6 +24,15 @@ int sm_count() {
     return cached[dev];
 }
 
+int64_t persistent_grid(const void *func, int threads, size_t smem, int64_t work) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int64_t grid = (int64_t)sm_count() * per_sm;
+    if (grid > work) grid = work;
+    return grid < 1 ? 1 : grid;
+}
+
 }  // namespace gbla
 
 GBLA_API const char *gbla_status_string(gbla_status s) {

@@ -256,11 +256,7 @@ static gbla_status chol_launch(int n, int nrhs, T *A, int64_t sA, T *B, int64_t 
         cudaError_t e = cudaFuncSetAttribute(k_chol_cta<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return from_cuda(e);
     }
-    int per_sm = (int)((228 * 1024) / (smem + 1024));
-    if (per_sm < 1) per_sm = 1;
-    if (per_sm > 8) per_sm = 8;
-    int64_t grid = (int64_t)sm_count() * per_sm;
-    if (grid > batch) grid = batch;
+    const int64_t grid = persistent_grid(reinterpret_cast<const void *>(k_chol_cta<T>), CTA_THREADS, smem, batch);
     k_chol_cta<T><<<(unsigned)grid, CTA_THREADS, smem, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
     return launch_status();
 }

@@ -53,6 +53,11 @@ template <> __device__ __forceinline__ double dev_rsqrt<double>(double x) { retu
 // Number of SMs of the current device (cached per device ordinal).
 int sm_count();
 
+// Grid for a persistent kernel: the blocks that can be resident at once
+// (occupancy of `func` at this block size and dynamic shared memory, times
+// the SM count), at most `work` and at least 1.
+int64_t persistent_grid(const void *func, int threads, size_t smem, int64_t work);
+
 // Round x up to a multiple of m.
 __host__ __device__ constexpr int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 

@@ -583,10 +583,8 @@ static gbla_status svj_cta_launch(int m, int n, const T *A, int64_t sA, T *S, in
             cudaFuncSetAttribute(k_gesvj_cta<T, MR, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return from_cuda(e);
     }
-    int per_sm = (int)((200 * 1024) / (smem + 1024));
-    per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
-    int64_t grid = (int64_t)sm_count() * per_sm;
-    if (grid > batch) grid = batch;
+    const int64_t grid =
+        persistent_grid(reinterpret_cast<const void *>(k_gesvj_cta<T, MR, NR>), SVJ_CTA_THREADS, smem, batch);
     k_gesvj_cta<T, MR, NR><<<(unsigned)grid, SVJ_CTA_THREADS, smem, st>>>(
         m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, warm_budget, fallback, info, sweeps, batch);
     return launch_status();

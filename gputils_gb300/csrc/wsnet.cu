@@ -103,13 +103,29 @@ __global__ void k_ws_adam(int64_t np, float *p, const float *g, float *m, float 
     }
 }
 
-// X[b][f] = bf16(A_idx(b)[f]) (column-major vec of the matrix)
-__global__ void k_ws_pack(int nn, const float *A, int64_t sA, const int *idx, int batch, uint16_t *X) {
-    const int64_t total = (int64_t)batch * nn;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t b = e / nn, f = e % nn;
-        const int64_t src = idx ? idx[b] : b;
-        X[e] = tobf(A[src * sA + f]);
+// X[b][f] = bf16(A_idx(b)[f]) (column-major vec of the matrix).  Grid: x over
+// 8-element vectors of a matrix, y over matrices (in slices of 65535); one
+// thread converts 8 values with two 16-byte loads and one 16-byte store when
+// the matrix is 16-byte aligned (nn is a multiple of 8).
+__global__ void k_ws_pack(int nn, const float *__restrict__ A, int64_t sA, const int *__restrict__ idx, int b0,
+                          int batch, uint16_t *__restrict__ X) {
+    const int b = b0 + blockIdx.y;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= batch || 8 * v >= nn) return;
+    const int64_t src = idx ? idx[b] : b;
+    const float *a = A + src * sA + 8 * v;
+    uint16_t *x = X + (int64_t)b * nn + 8 * v;
+    if ((reinterpret_cast<uintptr_t>(a) & 15) == 0) {
+        const float4 p = reinterpret_cast<const float4 *>(a)[0], q = reinterpret_cast<const float4 *>(a)[1];
+        uint4 u;
+        u.x = (uint32_t)tobf(p.x) | ((uint32_t)tobf(p.y) << 16);
+        u.y = (uint32_t)tobf(p.z) | ((uint32_t)tobf(p.w) << 16);
+        u.z = (uint32_t)tobf(q.x) | ((uint32_t)tobf(q.y) << 16);
+        u.w = (uint32_t)tobf(q.z) | ((uint32_t)tobf(q.w) << 16);
+        *reinterpret_cast<uint4 *>(x) = u;
+    } else {
+#pragma unroll
+        for (int e = 0; e < 8; e++) x[e] = tobf(a[e]);
     }
 }
 
@@ -409,26 +425,86 @@ __global__ void __launch_bounds__(WS_T)
     }
 }
 
-// V0 for a batch: persistent blocks, Vb loaded once per block
-__global__ void __launch_bounds__(WS_T)
+// V0 for a batch, without forming the inverse: V0 = Vb (2 (I - S)^{-1} - I),
+// so V0^T = 2 (I + S)^{-1} Vb^T - Vb^T, and one Gauss-Jordan elimination of
+// [I + S | Vb^T] (64 x 128 in registers, the thread mapping of
+// sm_cayley_inverse; I + S also has symmetric part I, so no pivoting) leaves
+// Y = (I + S)^{-1} Vb^T in the right half.  Thread (row r, column c of Y)
+// writes V0[r n + c] = V0(c, r) = 2 Y(r, c) - Vb(c, r), contiguous in c.
+__global__ void __launch_bounds__(WS_T, 3)
     k_ws_frame(int n, int P, const float *__restrict__ out, const float *__restrict__ Vbase, float *__restrict__ V0g,
                int64_t sV0, int batch) {
-    extern __shared__ __align__(16) float wsm[];
-    float *X = wsm, *Vb = X + WS_MAT, *V0 = Vb + WS_MAT;
     __shared__ GJBuf gb;
-    const int tid = threadIdx.x;
-    for (int e = tid; e < n * n; e += WS_T) Vb[(e / n) * WS_LD + e % n] = Vbase[e];
-    __syncthreads();
+    const int t = threadIdx.x, r0 = (t & 15) * 4, c0 = (t >> 4) * 8;
     for (int b = blockIdx.x; b < batch; b += gridDim.x) {
-        sm_cayley_inverse(n, out + (int64_t)b * P, X, gb);
-        sm_frame(n, Vb, X, V0);
-        for (int e = tid; e < n * n; e += WS_T) V0g[(int64_t)b * sV0 + e] = V0[(e / n) * WS_LD + e % n];
+        const float *o = out + (int64_t)b * P;
+        float m[4][8];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int r = r0 + a, c = c0 + q;
+                float v;
+                if (c < 64) {
+                    v = r == c ? 1.0f : 0.0f;
+                    if (r < n && c < n && r != c) v = r < c ? o[upper_index(r, c, n)] : -o[upper_index(c, r, n)];
+                } else {
+                    // Vb^T(r, c - 64) = Vb(c - 64, r), column-major Vb
+                    v = (r < n && c - 64 < n) ? Vbase[r * n + (c - 64)] : 0.0f;
+                }
+                m[a][q] = v;
+            }
+        for (int kk = 0; kk < n; kk += 8) {
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int k = kk + q;
+                if (k >= n) break;
+                const int par = k & 1;
+                if (c0 == kk) {
+#pragma unroll
+                    for (int a = 0; a < 4; a++) gb.pcol[par][r0 + a] = m[a][q];
+                }
+                __syncthreads();
+                if (r0 == (k & ~3)) {
+                    const float inv = 1.0f / gb.pcol[par][k];
+#pragma unroll
+                    for (int qq = 0; qq < 8; qq++) {
+                        m[q & 3][qq] *= inv;
+                        gb.prow[par][c0 + qq] = m[q & 3][qq];
+                    }
+                }
+                __syncthreads();
+                float pr[8];
+#pragma unroll
+                for (int qq = 0; qq < 8; qq++) pr[qq] = gb.prow[par][c0 + qq];
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    if (r0 + a == k) continue;
+                    const float f = gb.pcol[par][r0 + a];
+#pragma unroll
+                    for (int qq = 0; qq < 8; qq++) m[a][qq] = fmaf(-f, pr[qq], m[a][qq]);
+                }
+            }
+        }
+        if (c0 >= 64) {
+            float *dst = V0g + (int64_t)b * sV0;
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int r = r0 + a;
+                if (r >= n) continue;
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int c = c0 - 64 + q;
+                    if (c < n) dst[r * n + c] = 2.0f * m[a][q] - Vbase[r * n + c];
+                }
+            }
+        }
         __syncthreads();
     }
 }
 
 constexpr size_t LOSS_SMEM = 7 * WS_MAT * sizeof(float);
-constexpr size_t FRAME_SMEM = 3 * WS_MAT * sizeof(float);
+constexpr size_t FRAME_SMEM = 0;
 
 unsigned grid_for(int64_t n, int threads) {
     int64_t g = (n + threads - 1) / threads;
@@ -474,8 +550,12 @@ gbla_status rowsum(int rows, int cols, const uint16_t *src, int64_t lds, float *
 // the backward pass needs are written too.
 gbla_status forward(gbla_wsnet *w, const float *A, int64_t sA, const int *idx, int batch, bool train,
                     cudaStream_t st) {
-    k_ws_pack<<<grid_for((int64_t)batch * w->in, 256), 256, 0, st>>>(w->in, A, sA, idx, batch, w->x);
-    WS_TRY(launch_status());
+    for (int b0 = 0; b0 < batch; b0 += 65535) {
+        const int nbat = batch - b0 < 65535 ? batch - b0 : 65535;
+        dim3 pg((unsigned)((w->in / 8 + 255) / 256), (unsigned)nbat);
+        k_ws_pack<<<pg, 256, 0, st>>>(w->in, A, sA, idx, b0, batch, w->x);
+        WS_TRY(launch_status());
+    }
     if (train) WS_TRY(transpose(batch, w->in, w->x, w->in, w->xt, w->ldb, st));
     gbla_bf16_epilogue e = epilogue();
     e.bias = w->param + w->o_b1;
@@ -725,7 +805,9 @@ GBLA_API gbla_status gbla_wsnet_predict(gbla_wsnet *w, const float *A, int64_t s
     for (int b0 = 0; b0 < batch; b0 += w->maxb) {
         const int nb = batch - b0 < w->maxb ? batch - b0 : w->maxb;
         WS_TRY(forward(w, A + (int64_t)b0 * sA, sA, nullptr, nb, false, st));
-        const int grid = nb < sm_count() * 4 ? nb : sm_count() * 4;
+        // persistent blocks: exactly the resident count, so no block waits for
+        // another's whole loop to finish
+        const int grid = (int)persistent_grid(reinterpret_cast<const void *>(k_ws_frame), WS_T, FRAME_SMEM, nb);
         k_ws_frame<<<(unsigned)grid, WS_T, FRAME_SMEM, st>>>(w->n, w->P, w->out, w->vbase, V0 + (int64_t)b0 * sV0, sV0,
                                                            nb);
         WS_TRY(launch_status());

@@ -204,8 +204,8 @@ class WarmStartNet:
 
 
 def train_family_model(n: int = 64, family_seed: int = 6, pairs: int = 200_000, epochs: int = 20,
-                       hidden: int = 512, batch: int = 512, lr: float = 1e-3, tol: float = 1e-6,
-                       theta_seed: int = 1234, seed: int = 0, log=None):
+                       hidden: int = 512, batch: int = 256, lr: float = 1e-3, tol: float = 1e-6,
+                       theta_seed: int = 1234, seed: int = 0, infer_batch: int = 32768, log=None):
     """Generate `pairs` (A, V) pairs of the parametric family with the cold
     Jacobi SVD, set the base frame to the family's A0 frame, train, and set
     the warm budget to the median cold sweep count.  Returns (net, stats)."""
@@ -221,7 +221,8 @@ def train_family_model(n: int = 64, family_seed: int = 6, pairs: int = 200_000, 
     sweeps = torch.cat(sweeps)
     A0 = torch.tensor(basis[0].T.copy(), device="cuda", dtype=torch.float32).reshape(1, n, n).contiguous()
     _, Vb, _, _ = jacobi(A0, tol=tol)
-    net = WarmStartNet(n, hidden, max_batch=max(batch, 4096), seed=seed)
+    # buffers sized for inference on a whole benchmark batch in one pass
+    net = WarmStartNet(n, hidden, max_batch=max(batch, infer_batch), seed=seed)
     net.set_base(Vb[0])
     hist = net.fit(A, V, epochs=epochs, batch=batch, lr=lr, seed=seed, log=log)
     net.warm_budget = int(sweeps.float().median().item())
