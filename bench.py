@@ -809,6 +809,11 @@ def run_ours_svd(args, dev, st, L, rank, world, dist):
     Sh = S.cpu().numpy().reshape(k, nmat)
     So = O.gesvj(Ah[idx], tol=1e-12)["S"]
     err = rel_err(Sh[idx][:, None, :], So[:, None, :])
+    e2e = _e2e_leg([np.ascontiguousarray(Ah.transpose(0, 2, 1))],
+                   lambda ins: (L.gbla_sgesvj_batched(nmat, nmat, ins[0].data_ptr(), nmat * nmat, S.data_ptr(), nmat,
+                                                      Vt.data_ptr(), nmat * nmat, None, 0, None, 0, 1e-6, 60,
+                                                      info.data_ptr(), sweeps.data_ptr(), k, st),),
+                   lambda ins: [S, Vt], k, args, world, dist, dev)
     reflib = None
     if not args.no_reference_library:
         try:
@@ -828,7 +833,7 @@ def run_ours_svd(args, dev, st, L, rank, world, dist):
                      "kernel": "gesvj", "algorithmic_flops_per_launch": flops,
                      "peak_source": "measured FFMA rate (gbla_diag_fma_throughput)"},
         "max_rel_err_vs_fp64": {"sigma": err}, "sweeps": {"mean": float(sw.mean()), "max": int(sw.max())},
-        "gpu_launches": args.steps, "clocks": clk.summary(), "reference_library": reflib, "e2e": None,
+        "gpu_launches": args.steps, "clocks": clk.summary(), "reference_library": reflib, "e2e": e2e,
     }
 
 
@@ -1019,6 +1024,46 @@ def reference_library_svd(dev, st, A0, Ah, nmat, sample):
             "calls": f"host loop of cusolverDnSgesvd('N','A'), {sample} calls timed, scaled linearly"}
 
 
+def _e2e_leg(host_inputs, call, outputs, units, args, world, dist, dev):
+    """The step through the C ABI with host buffers: every step copies the
+    inputs from pinned host memory, runs `call` on the device copies and copies
+    `outputs(device inputs)` back to pinned host memory; timed with CUDA events
+    over max(3, min(steps, 10)) steps after two untimed ones."""
+    import torch
+    from gputils_gb300 import _lib
+
+    hin = [torch.from_numpy(np.ascontiguousarray(h)).pin_memory() for h in host_inputs]
+    din = [torch.empty(h.shape, dtype=h.dtype, device=dev) for h in hin]
+    hout = None
+
+    def one():
+        nonlocal hout
+        for d, h in zip(din, hin):
+            d.copy_(h, non_blocking=True)
+        for status in call(din):
+            _lib.check(status, "e2e")
+        outs = outputs(din)
+        if hout is None:
+            hout = [torch.empty(o.shape, dtype=o.dtype).pin_memory() for o in outs]
+        for h, o in zip(hout, outs):
+            h.copy_(o, non_blocking=True)
+
+    for _ in range(2):
+        one()
+    torch.cuda.synchronize()
+    steps = max(3, min(args.steps, 10))
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(steps):
+        one()
+    f1.record()
+    torch.cuda.synchronize()
+    t, _ = aggregate(f0.elapsed_time(f1) / 1e3 / steps, 0.0, world, dist, dev)
+    return {"value": units * world / t, "unit": "matrices/s",
+            "h2d_bytes_per_step": int(sum(h.numel() * h.element_size() for h in hin)),
+            "d2h_bytes_per_step": int(sum(h.numel() * h.element_size() for h in hout)), "ms_per_step": t * 1e3}
+
+
 def run_ours_d1(args, dev, st, L, rank, world, dist):
     """CholeskyBatchFactoriser factorise() + solve() on 4096 16x16: the
     reference API path (2 launches: potrf, potrs)."""
@@ -1055,6 +1100,10 @@ def run_ours_d1(args, dev, st, L, rank, world, dist):
     idx = np.arange(0, k, 16)
     _, xo, _ = O.posv(M[idx], b[idx])
     err = rel_err(x[idx], xo)
+    e2e = _e2e_leg([np.ascontiguousarray(M.transpose(0, 2, 1)), np.ascontiguousarray(b.transpose(0, 2, 1))],
+                   lambda ins: (L.gbla_spotrf_batched(n, ins[0].data_ptr(), n * n, info.data_ptr(), k, st),
+                                L.gbla_spotrs_batched(n, 1, ins[0].data_ptr(), n * n, ins[1].data_ptr(), n, k, st)),
+                   lambda ins: [ins[1]], k, args, world, dist, dev)
     reflib = None
     if not args.no_reference_library:
         try:
@@ -1093,7 +1142,7 @@ def run_ours_d1(args, dev, st, L, rank, world, dist):
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": ach / pk["hbm_gbs"], "traffic": traffic_for("chol_d1"), "kernel": "potrf+potrs"},
         "max_rel_err_vs_fp64": {"x": err}, "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
-        "e2e": None, "reference_library": reflib,
+        "e2e": e2e, "reference_library": reflib,
     }
 
 
