@@ -138,10 +138,9 @@ __global__ void __launch_bounds__(128, 1)
 template <typename T>
 __host__ __device__ inline size_t ragged_large_smem(int nmax, int warps) {
     const int ld = cta_ld(nmax);
-    // panel rows (n x 8, 16-byte aligned) + float factor (n x ld) + float dinv (n, padded to
-    // an even count so that x stays 8-byte aligned) + T x (warps x n)
-    return sizeof(float) * ((size_t)nmax * 8 + (size_t)nmax * ld + (size_t)round_up(nmax, 2)) +
-           sizeof(T) * (size_t)warps * nmax + 64;
+    (void)warps;
+    // two panel-row buffers (n x 8 each, 16-byte aligned) + float factor (n x ld) + float dinv (n)
+    return sizeof(float) * ((size_t)nmax * 16 + (size_t)nmax * ld + (size_t)nmax) + 64;
 }
 
 // Solve L L^T x = b for one column held in registers (element lane + 32 t in
@@ -187,6 +186,93 @@ __device__ __forceinline__ void reg_solve(const float *__restrict__ a, int ld, c
 
 constexpr int RG_PANEL = 8;
 
+// Warp 0: factor the panel of columns [k0, k0 + pw) (rows k0 .. n-1, held in
+// registers as rows k0 + lane + 32 t), write it back into the factor and,
+// row-major, into pbuf for the rank-8 updates.
+__device__ __forceinline__ void panel_factor(float *__restrict__ a, int ld, int n, int k0, int pw,
+                                             float *__restrict__ pbuf, float *__restrict__ dinv, int *s_fail,
+                                             int lane) {
+    float pv[4][RG_PANEL];
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+#pragma unroll
+        for (int c = 0; c < RG_PANEL; c++) {
+            const int r = k0 + lane + 32 * t;
+            pv[t][c] = (c < pw && r < n) ? a[(k0 + c) * ld + r] : 0.f;
+        }
+#pragma unroll
+    for (int c = 0; c < RG_PANEL; c++) {
+        if (c >= pw) break;
+        const int k = k0 + c;
+        const float d = shfl(pv[0][c], c);  // row k sits in lane c, t = 0
+        if (!(d > 0.f) && lane == 0 && *s_fail == 0) *s_fail = k + 1;
+        const float l = sqrtf(d), il = 1.f / l;
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int r = k0 + lane + 32 * t;
+            if (r > k) pv[t][c] *= il;
+        }
+        if (lane == c) pv[0][c] = l;
+        if (lane == 0) dinv[k] = il;
+#pragma unroll
+        for (int c2 = c + 1; c2 < RG_PANEL; c2++) {
+            if (c2 >= pw) break;
+            const float ljk = shfl(pv[0][c], c2);  // L(k0 + c2, k)
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int r = k0 + lane + 32 * t;
+                if (r >= k0 + c2) pv[t][c2] = fmaf(-pv[t][c], ljk, pv[t][c2]);
+            }
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const int r = k0 + lane + 32 * t;
+        if (r >= n) continue;
+#pragma unroll
+        for (int c = 0; c < RG_PANEL; c++)
+            if (c < pw && r >= k0 + c) a[(k0 + c) * ld + r] = pv[t][c];
+        // the panel's rows for the rank-8 updates, row-major (zero past pw)
+        float4 *pr = reinterpret_cast<float4 *>(pbuf + 8 * r);
+        pr[0] = make_float4(pv[t][0], pw > 1 ? pv[t][1] : 0.f, pw > 2 ? pv[t][2] : 0.f, pw > 3 ? pv[t][3] : 0.f);
+        pr[1] = make_float4(pw > 4 ? pv[t][4] : 0.f, pw > 5 ? pv[t][5] : 0.f, pw > 6 ? pv[t][6] : 0.f,
+                            pw > 7 ? pv[t][7] : 0.f);
+    }
+}
+
+// Rank-8 update of the lower-triangle columns j = j_lo + wi, + ws, ... < j_hi
+// (rows j .. n-1) with the panel rows in pbuf: increasing k, one fma each
+// (zeros past the panel width leave the value unchanged).
+__device__ __forceinline__ void panel_update(float *__restrict__ a, int ld, int n, const float *__restrict__ pbuf,
+                                             int j_lo, int j_hi, int wi, int ws, int lane) {
+    for (int j = j_lo + wi; j < j_hi; j += ws) {
+        const float4 lj0 = reinterpret_cast<const float4 *>(pbuf + 8 * j)[0];
+        const float4 lj1 = reinterpret_cast<const float4 *>(pbuf + 8 * j)[1];
+        float *colj = a + j * ld;
+        for (int i = j + lane; i < n; i += 32) {
+            const float4 li0 = reinterpret_cast<const float4 *>(pbuf + 8 * i)[0];
+            const float4 li1 = reinterpret_cast<const float4 *>(pbuf + 8 * i)[1];
+            float acc = colj[i];
+            acc = fmaf(-li0.x, lj0.x, acc);
+            acc = fmaf(-li0.y, lj0.y, acc);
+            acc = fmaf(-li0.z, lj0.z, acc);
+            acc = fmaf(-li0.w, lj0.w, acc);
+            acc = fmaf(-li1.x, lj1.x, acc);
+            acc = fmaf(-li1.y, lj1.y, acc);
+            acc = fmaf(-li1.z, lj1.z, acc);
+            acc = fmaf(-li1.w, lj1.w, acc);
+            colj[i] = acc;
+        }
+    }
+}
+
+// x_j of a right-hand side held in registers (row lane + 32 t in x[t]), for
+// j = 32 tk + lk with tk known at compile time
+template <typename T>
+__device__ __forceinline__ T xget(const T (&x)[4], int tk, int lk) {
+    return shfl(tk == 0 ? x[0] : tk == 1 ? x[1] : tk == 2 ? x[2] : x[3], lk);
+}
+
 // at least 3 blocks of 256 (6 of 128, 12 of 64, 1 of 512) per SM: register cap ~85
 template <typename T, int THREADS>
 __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
@@ -197,102 +283,46 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
     const RaggedSys s = sys[first + blockIdx.x];
     const int n = s.n, nrhs = s.nrhs, ld = cta_ld(n);
     const int ldmax = cta_ld(nmax);
-    float *prow = reinterpret_cast<float *>(rsm);  // panel row r at prow[8 r .. 8 r + 7]
-    float *a = prow + (size_t)nmax * 8;
+    float *pbuf0 = reinterpret_cast<float *>(rsm);  // panel row r at pbuf[8 r .. 8 r + 7]
+    float *pbuf1 = pbuf0 + (size_t)nmax * 8;
+    float *a = pbuf1 + (size_t)nmax * 8;
     float *dinv = a + (size_t)nmax * ldmax;
-    T *xs = reinterpret_cast<T *>(dinv + round_up(nmax, 2) + ((nmax * 8 + (size_t)nmax * ldmax) & 1));
     __shared__ int s_fail;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const T *ag = A_in + s.a_off;
 
     for (int j = warp; j < n; j += RG_LARGE_WARPS)
-        for (int i = j + lane; i < n; i += 32) a[(int64_t)j * ld + i] = (float)ag[(int64_t)j * n + i];
+        for (int i = j + lane; i < n; i += 32) a[j * ld + i] = (float)ag[(int64_t)j * n + i];
     if (threadIdx.x == 0) s_fail = 0;
     __syncthreads();
-    // Blocked right-looking factorisation: warp 0 factors a panel of 8
-    // columns in registers (rows k0 + lane + 32 t), then every warp applies
-    // the panel's rank-8 update to the trailing lower triangle.  Each
-    // element receives its updates in increasing k with one fma each, as in
-    // the column-by-column algorithm.  Two barriers per panel.
-    for (int k0 = 0; k0 < n; k0 += RG_PANEL) {
+    // Blocked right-looking factorisation with look-ahead: while warps 1..W-1
+    // apply panel p's rank-8 update to the columns past panel p + 1, warp 0
+    // applies it to panel p + 1's columns and factors panel p + 1 (into the
+    // other panel buffer).  Each element still receives its updates in
+    // increasing k with one fma each, as in the column-by-column algorithm.
+    // One barrier per panel.
+    if (warp == 0) panel_factor(a, ld, n, 0, n < RG_PANEL ? n : RG_PANEL, pbuf0, dinv, &s_fail, lane);
+    __syncthreads();
+    for (int k0 = 0, p = 0; k0 < n; k0 += RG_PANEL, p++) {
         const int pw = n - k0 < RG_PANEL ? n - k0 : RG_PANEL;
+        const int kn = k0 + pw, pwn = n - kn < RG_PANEL ? n - kn : RG_PANEL;  // next panel
+        const float *pb = (p & 1) ? pbuf1 : pbuf0;
+        float *pnext = (p & 1) ? pbuf0 : pbuf1;
         if (warp == 0) {
-            float pv[4][RG_PANEL];
-#pragma unroll
-            for (int t = 0; t < 4; t++)
-#pragma unroll
-                for (int c = 0; c < RG_PANEL; c++) {
-                    const int r = k0 + lane + 32 * t;
-                    pv[t][c] = (c < pw && r < n) ? a[(int64_t)(k0 + c) * ld + r] : 0.f;
-                }
-#pragma unroll
-            for (int c = 0; c < RG_PANEL; c++) {
-                if (c >= pw) break;
-                const int k = k0 + c;
-                const float d = shfl(pv[0][c], c);  // row k sits in lane c, t = 0
-                if (!(d > 0.f) && lane == 0 && s_fail == 0) s_fail = k + 1;
-                const float l = sqrtf(d), il = 1.f / l;
-#pragma unroll
-                for (int t = 0; t < 4; t++) {
-                    const int r = k0 + lane + 32 * t;
-                    if (r > k) pv[t][c] *= il;
-                }
-                if (lane == c) pv[0][c] = l;
-                if (lane == 0) dinv[k] = il;
-#pragma unroll
-                for (int c2 = c + 1; c2 < RG_PANEL; c2++) {
-                    if (c2 >= pw) break;
-                    const float ljk = shfl(pv[0][c], c2);  // L(k0 + c2, k)
-#pragma unroll
-                    for (int t = 0; t < 4; t++) {
-                        const int r = k0 + lane + 32 * t;
-                        if (r >= k0 + c2) pv[t][c2] = fmaf(-pv[t][c], ljk, pv[t][c2]);
-                    }
-                }
+            if (pwn > 0) {
+                panel_update(a, ld, n, pb, kn, kn + pwn, 0, 1, lane);
+                __syncwarp();
+                panel_factor(a, ld, n, kn, pwn, pnext, dinv, &s_fail, lane);
             }
-#pragma unroll
-            for (int t = 0; t < 4; t++) {
-                const int r = k0 + lane + 32 * t;
-                if (r >= n) continue;
-#pragma unroll
-                for (int c = 0; c < RG_PANEL; c++)
-                    if (c < pw && r >= k0 + c) a[(k0 + c) * ld + r] = pv[t][c];
-                // the panel's rows for the trailing update, row-major (zero past pw)
-                float4 *pr = reinterpret_cast<float4 *>(prow + 8 * r);
-                pr[0] = make_float4(pv[t][0], pw > 1 ? pv[t][1] : 0.f, pw > 2 ? pv[t][2] : 0.f,
-                                    pw > 3 ? pv[t][3] : 0.f);
-                pr[1] = make_float4(pw > 4 ? pv[t][4] : 0.f, pw > 5 ? pv[t][5] : 0.f, pw > 6 ? pv[t][6] : 0.f,
-                                    pw > 7 ? pv[t][7] : 0.f);
-            }
-        }
-        __syncthreads();
-        const int kend = k0 + pw;
-        for (int j = kend + warp; j < n; j += RG_LARGE_WARPS) {
-            const float4 lj0 = reinterpret_cast<const float4 *>(prow + 8 * j)[0];
-            const float4 lj1 = reinterpret_cast<const float4 *>(prow + 8 * j)[1];
-            float *colj = a + j * ld;
-            for (int i = j + lane; i < n; i += 32) {
-                const float4 li0 = reinterpret_cast<const float4 *>(prow + 8 * i)[0];
-                const float4 li1 = reinterpret_cast<const float4 *>(prow + 8 * i)[1];
-                float acc = colj[i];
-                // increasing k, one fma each (zeros past pw leave acc unchanged)
-                acc = fmaf(-li0.x, lj0.x, acc);
-                acc = fmaf(-li0.y, lj0.y, acc);
-                acc = fmaf(-li0.z, lj0.z, acc);
-                acc = fmaf(-li0.w, lj0.w, acc);
-                acc = fmaf(-li1.x, lj1.x, acc);
-                acc = fmaf(-li1.y, lj1.y, acc);
-                acc = fmaf(-li1.z, lj1.z, acc);
-                acc = fmaf(-li1.w, lj1.w, acc);
-                colj[i] = acc;
-            }
+        } else {
+            panel_update(a, ld, n, pb, kn + pwn, n, warp - 1, RG_LARGE_WARPS - 1, lane);
         }
         __syncthreads();
     }
     if (threadIdx.x == 0 && info) info[s.orig] = s_fail;
 
     T *bg = B + s.b_off;
-    T *x = xs + (size_t)warp * nmax;
+    const int nt = (n + 31) >> 5;
     for (int c = warp; c < nrhs; c += RG_LARGE_WARPS) {
         const T *bc = bg + (int64_t)c * n;
         float w[4];
@@ -302,15 +332,12 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
             w[t] = i < n ? (float)bc[i] : 0.f;
         }
         reg_solve(a, ld, dinv, w, n, lane);
+        T x[4];  // the solution, rows lane + 32 t, in the precision of the data
 #pragma unroll
-        for (int t = 0; t < 4; t++) {
-            const int i = lane + 32 * t;
-            if (i < n) x[i] = (T)w[t];
-        }
-        __syncwarp();
+        for (int t = 0; t < 4; t++) x[t] = (T)w[t];
         for (int it = 0; it < refine; it++) {
-            // r = b - A x with the full symmetric A; rows lane + 32 t; the
-            // columns of A are loaded four at a time to keep loads in flight
+            // r = b - A x with the full symmetric A; rows lane + 32 t; A's
+            // columns four at a time, x_j by shuffle
             if constexpr (sizeof(T) == 4) {
                 ff acc[4];
 #pragma unroll
@@ -319,31 +346,37 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
                     acc[t].h = i < n ? (float)bc[i] : 0.f;
                     acc[t].l = 0.f;
                 }
-                const int nt = (n + 31) >> 5;
-                int j = 0;
-                for (; j + 4 <= n; j += 4) {
-                    float av[4][4];
 #pragma unroll
-                    for (int q = 0; q < 4; q++)
+                for (int tk = 0; tk < 4; tk++) {
+                    if (tk >= nt) break;
+                    const int kmax = n - 32 * tk < 32 ? n - 32 * tk : 32;
+                    int lk = 0;
+                    for (; lk + 4 <= kmax; lk += 4) {
+                        const int j = 32 * tk + lk;
+                        float av[4][4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+#pragma unroll
+                            for (int t = 0; t < 4; t++) {
+                                const int i = lane + 32 * t;
+                                av[q][t] = (t < nt && i < n) ? (float)ag[(int64_t)(j + q) * n + i] : 0.f;
+                            }
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            const float xj = (float)xget(x, tk, lk + q);
+#pragma unroll
+                            for (int t = 0; t < 4; t++)
+                                if (t < nt) ff_fma(acc[t], -av[q][t], xj, 0.f);
+                        }
+                    }
+                    for (; lk < kmax; lk++) {
+                        const int j = 32 * tk + lk;
+                        const float xj = (float)xget(x, tk, lk);
 #pragma unroll
                         for (int t = 0; t < 4; t++) {
                             const int i = lane + 32 * t;
-                            av[q][t] = (t < nt && i < n) ? (float)ag[(int64_t)(j + q) * n + i] : 0.f;
+                            if (t < nt && i < n) ff_fma(acc[t], -(float)ag[(int64_t)j * n + i], xj, 0.f);
                         }
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const float xj = (float)x[j + q];
-#pragma unroll
-                        for (int t = 0; t < 4; t++)
-                            if (t < nt) ff_fma(acc[t], -av[q][t], xj, 0.f);
-                    }
-                }
-                for (; j < n; j++) {
-                    const float xj = (float)x[j];
-#pragma unroll
-                    for (int t = 0; t < 4; t++) {
-                        const int i = lane + 32 * t;
-                        if (i < n) ff_fma(acc[t], -(float)ag[(int64_t)j * n + i], xj, 0.f);
                     }
                 }
 #pragma unroll
@@ -355,55 +388,59 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
                     const int i = lane + 32 * t;
                     acc[t] = i < n ? (double)bc[i] : 0.0;
                 }
-                const int nt = (n + 31) >> 5;
-                int j = 0;
-                for (; j + 4 <= n; j += 4) {
-                    double av[4][4];
 #pragma unroll
-                    for (int q = 0; q < 4; q++)
+                for (int tk = 0; tk < 4; tk++) {
+                    if (tk >= nt) break;
+                    const int kmax = n - 32 * tk < 32 ? n - 32 * tk : 32;
+                    int lk = 0;
+                    for (; lk + 4 <= kmax; lk += 4) {
+                        const int j = 32 * tk + lk;
+                        double av[4][4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+#pragma unroll
+                            for (int t = 0; t < 4; t++) {
+                                const int i = lane + 32 * t;
+                                av[q][t] = (t < nt && i < n) ? (double)ag[(int64_t)(j + q) * n + i] : 0.0;
+                            }
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            const double xj = (double)xget(x, tk, lk + q);
+#pragma unroll
+                            for (int t = 0; t < 4; t++)
+                                if (t < nt) acc[t] = fma(-av[q][t], xj, acc[t]);
+                        }
+                    }
+                    for (; lk < kmax; lk++) {
+                        const int j = 32 * tk + lk;
+                        const double xj = (double)xget(x, tk, lk);
 #pragma unroll
                         for (int t = 0; t < 4; t++) {
                             const int i = lane + 32 * t;
-                            av[q][t] = (t < nt && i < n) ? (double)ag[(int64_t)(j + q) * n + i] : 0.0;
+                            if (t < nt && i < n) acc[t] = fma(-(double)ag[(int64_t)j * n + i], xj, acc[t]);
                         }
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const double xj = (double)x[j + q];
-#pragma unroll
-                        for (int t = 0; t < 4; t++)
-                            if (t < nt) acc[t] = fma(-av[q][t], xj, acc[t]);
-                    }
-                }
-                for (; j < n; j++) {
-                    const double xj = (double)x[j];
-#pragma unroll
-                    for (int t = 0; t < 4; t++) {
-                        const int i = lane + 32 * t;
-                        if (i < n) acc[t] = fma(-(double)ag[(int64_t)j * n + i], xj, acc[t]);
                     }
                 }
 #pragma unroll
                 for (int t = 0; t < 4; t++) w[t] = (float)acc[t];
             }
             reg_solve(a, ld, dinv, w, n, lane);
-            __syncwarp();
 #pragma unroll
-            for (int t = 0; t < 4; t++) {
-                const int i = lane + 32 * t;
-                if (i < n) x[i] = x[i] + (T)w[t];
-            }
-            __syncwarp();
+            for (int t = 0; t < 4; t++) x[t] = x[t] + (T)w[t];
         }
         T *bo = bg + (int64_t)c * n;
-        for (int i = lane; i < n; i += 32) bo[i] = x[i];
-        __syncwarp();
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int i = lane + 32 * t;
+            if (i < n) bo[i] = x[t];
+        }
     }
     // L (lower triangle, FP32 factor) back in place, once every warp has
     // finished reading the original A for its residuals
     __syncthreads();
     T *aw = A + s.a_off;
     for (int j = warp; j < n; j += RG_LARGE_WARPS)
-        for (int i = j + lane; i < n; i += 32) aw[(int64_t)j * n + i] = (T)a[(int64_t)j * ld + i];
+        for (int i = j + lane; i < n; i += 32) aw[(int64_t)j * n + i] = (T)a[j * ld + i];
 }
 
 // Bucket the large class (plan order: largest n first) by cfg.bucket_width:

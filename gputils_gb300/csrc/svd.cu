@@ -164,23 +164,34 @@ __global__ void __launch_bounds__(128, 1)
     for (sweep = 1; sweep <= limit; sweep++) {
         total++;
         int rotated = 0;
-        for (int r = 0; r < N - 1; r++) {
-            const int partner = rr_partner(lane, r, N);
+        // this lane's column norm, recomputed once per sweep and carried through
+        // the rotations (alpha - t gamma for column p, beta + t gamma for q)
+        T own = 0.f;
+#pragma unroll
+        for (int i = 0; i < MR; i++) own = fma(a[i], a[i], own);
+        const int M = N - 1;
+        for (int r = 0; r < M; r++) {
+            // round-robin partner without integer division (N even, M = N - 1 odd)
+            int partner;
+            if (lane == M) partner = (r & 1) ? (r + M) >> 1 : r >> 1;
+            else if (lane > M) partner = lane;
+            else {
+                partner = r - lane;
+                if (partner < 0) partner += M;
+                if (partner == lane) partner = M;
+            }
             const bool active = col && partner < n && partner != lane;
-            T alpha = 0.f, gamma = 0.f;
+            T gamma = 0.f;
             T o[MR];
 #pragma unroll
-            for (int i = 0; i < MR; i++) {
-                o[i] = shfl(a[i], partner);
-                alpha = fma(a[i], a[i], alpha);
-            }
-            const T beta_o = shfl(alpha, partner);
+            for (int i = 0; i < MR; i++) o[i] = shfl(a[i], partner);
+            const T beta_o = shfl(own, partner);
             const bool low = lane < partner;  // this lane holds column p of the pair
 #pragma unroll
             for (int i = 0; i < MR; i++) gamma = fma(low ? a[i] : o[i], low ? o[i] : a[i], gamma);
-            T c = 1.f, s = 0.f;
-            const T ap = low ? alpha : beta_o, aq = low ? beta_o : alpha;
-            bool rot = active && jacobi_rotation<T>(ap, aq, gamma, tol, small, c, s);
+            T c = 1.f, s = 0.f, t = 0.f;
+            const T ap = low ? own : beta_o, aq = low ? beta_o : own;
+            bool rot = active && jacobi_rotation_t<T>(ap, aq, gamma, tol, small, c, s, t);
             // a_p' = c a_p - s a_q ; a_q' = s a_p + c a_q
             const T cm = c, so = low ? -s : s;
             T ov[32];
@@ -191,6 +202,7 @@ __global__ void __launch_bounds__(128, 1)
                 for (int i = 0; i < MR; i++) a[i] = fma(cm, a[i], so * o[i]);
 #pragma unroll
                 for (int i = 0; i < 32; i++) v[i] = fma(cm, v[i], so * ov[i]);
+                own = low ? fma(-t, gamma, own) : fma(t, gamma, own);
             }
             rotated |= rot;
         }
