@@ -69,9 +69,16 @@ __global__ void __launch_bounds__(128, 1) k_chol_lanerow(int n, int nrhs, T *__r
     }
     if (mode & CH_SOLVE) {
         T *b_g = B + (act ? mat : 0) * sB;
+        // a stored factor (solve-only call): also read it by columns, so the
+        // transposed substitution needs no reductions
+        T at[NB];
+        if (!(mode & CH_FACTOR)) {
+#pragma unroll
+            for (int k = 0; k < NB; k++) at[k] = (rowok && k < n && k >= r) ? a_g[(int64_t)r * n + k] : T(0);
+        }
         for (int c = 0; c < nrhs; c++) {
             T b = rowok ? b_g[(int64_t)c * n + r] : T(0);
-            T x = lr_solve<T, NB>(a, dinv, b, n, r);
+            T x = (mode & CH_FACTOR) ? lr_solve<T, NB>(a, dinv, b, n, r) : lr_solve_cols<T, NB>(a, at, dinv, b, n, r);
             if ((mode & CH_FACTOR) && refine > 0) {
                 R xr = R(x);
                 for (int it = 0; it < refine; it++) {

@@ -15,8 +15,18 @@ __device__ __forceinline__ void lr_factor(T (&a)[NB], T &dinv, int &fail, int n,
         if (k < n) {
             T d = shfl(a[k], k, NB);
             if (!(d > T(0)) && fail == 0) fail = k + 1;
-            T l = dev_sqrt<T>(d);
-            T il = T(1) / l;
+            T l, il;
+            if constexpr (sizeof(T) == 4) {
+                // reciprocal square root with one Newton step (about 1 ulp),
+                // l = d / sqrt(d): a short dependency chain per pivot
+                float y = rsqrtf(d);
+                y = y * fmaf(-0.5f * d * y, y, 1.5f);
+                il = y;
+                l = d * y;
+            } else {
+                l = dev_sqrt<T>(d);
+                il = T(1) / l;
+            }
             if (r == k) { a[k] = l; dinv = il; }
             else if (r > k) a[k] *= il;
 #pragma unroll
@@ -47,6 +57,30 @@ __device__ __forceinline__ T lr_solve(const T (&a)[NB], T dinv, T b, int n, int 
             T part = (r > k && r < n) ? a[k] * b : T(0);
             T s = group_sum(part, NB);
             if (r == k) b = (b - s) * dinv;
+        }
+    }
+    return b;
+}
+
+// Solve L L^T x = b with L available both by rows (a: row r in lane r) and by
+// columns (at[k] = L(k, r) in lane r): both substitutions are column-oriented,
+// one broadcast and one fma per step.
+template <typename T, int NB>
+__device__ __forceinline__ T lr_solve_cols(const T (&a)[NB], const T (&at)[NB], T dinv, T b, int n, int r) {
+#pragma unroll
+    for (int k = 0; k < NB; k++) {
+        if (k < n) {
+            if (r == k) b *= dinv;
+            T yk = shfl(b, k, NB);
+            if (r > k) b -= a[k] * yk;
+        }
+    }
+#pragma unroll
+    for (int k = NB - 1; k >= 0; k--) {
+        if (k < n) {
+            if (r == k) b *= dinv;
+            T xk = shfl(b, k, NB);
+            if (r < k) b -= at[k] * xk;
         }
     }
     return b;
