@@ -50,6 +50,10 @@ __global__ void __launch_bounds__(128, 1) k_chol_lanerow(int n, int nrhs, T *__r
     const bool act = mat < batch;
     const bool rowok = act && r < n;
     T *a_g = A + (act ? mat : 0) * sA;
+    // launched with programmatic stream serialization: let the next kernel
+    // begin launching, and wait for the previous one before reading memory
+    asm volatile("griddepcontrol.launch_dependents;");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 
     T a[NB];
 #pragma unroll
@@ -250,12 +254,27 @@ static gbla_status chol_launch(int n, int nrhs, T *A, int64_t sA, T *B, int64_t 
         int mpb = 4 * (32 / nb);
         int64_t grid = (batch + mpb - 1) / mpb;
         if (grid > 0x7fffffff) return GBLA_INVALID_VALUE;
+        // programmatic dependent launch: the kernel may start while the
+        // previous kernel on the stream drains; it waits for it (and its
+        // memory) before touching global memory (griddepcontrol.wait)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3(128);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaError_t e;
         if (nb == 8)
-            k_chol_lanerow<T, 8><<<(unsigned)grid, 128, 0, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+            e = cudaLaunchKernelEx(&cfg, k_chol_lanerow<T, 8>, n, nrhs, A, sA, B, sB, info, mode, refine, batch);
         else if (nb == 16)
-            k_chol_lanerow<T, 16><<<(unsigned)grid, 128, 0, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+            e = cudaLaunchKernelEx(&cfg, k_chol_lanerow<T, 16>, n, nrhs, A, sA, B, sB, info, mode, refine, batch);
         else
-            k_chol_lanerow<T, 32><<<(unsigned)grid, 128, 0, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+            e = cudaLaunchKernelEx(&cfg, k_chol_lanerow<T, 32>, n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+        if (e != cudaSuccess) return from_cuda(e);
         return launch_status();
     }
     size_t smem = cta_smem_bytes<T>(n);
