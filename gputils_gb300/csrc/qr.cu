@@ -192,11 +192,11 @@ struct QrWarp {
 };
 
 // Augmented-system refinement of one right-hand side (FP32 data, double-FP32
-// residuals).  x0: FP32 solution in lane j; returns the refined x in lane j.
-template <int R>
-__device__ __forceinline__ float refine_ls(const QrWarp<float, R> &q, const float *A0, int m, int n,
+// residuals).  A0: the original matrix, column stride lda; x0: FP32 solution
+// in lane j; returns the refined x in lane j.
+template <int R, class QF>
+__device__ __forceinline__ float refine_ls(const QF &q, const float *A0, int lda, int m, int n,
                                            const float (&b)[R], float x0, const float *tau_s, int refine) {
-    constexpr int LDM = 32 * R;
     const int lane = q.lane;
     float xh = x0, xl = 0.f;
     float rh[R], rl[R];
@@ -220,7 +220,7 @@ __device__ __forceinline__ float refine_ls(const QrWarp<float, R> &q, const floa
 #pragma unroll
                 for (int t = 0; t < R; t++) {
                     int r = lane + 32 * t;
-                    float aij = r < m ? A0[j * LDM + r] : 0.f;
+                    float aij = r < m ? A0[(int64_t)j * lda + r] : 0.f;
                     ff_fma(f[t], -aij, xjh, xjl);
                 }
             }
@@ -246,7 +246,7 @@ __device__ __forceinline__ float refine_ls(const QrWarp<float, R> &q, const floa
 #pragma unroll
                     for (int t = 0; t < R; t++) {
                         int r = lane + 32 * t;
-                        float aij = r < m ? A0[(j0 + c) * LDM + r] : 0.f;
+                        float aij = r < m ? A0[(int64_t)(j0 + c) * lda + r] : 0.f;
                         ff_fma(acc[c], aij, rh[t], rl[t]);
                     }
                 }
@@ -285,10 +285,13 @@ __device__ __forceinline__ float refine_ls(const QrWarp<float, R> &q, const floa
     return xh + xl;
 }
 
-template <typename T, int R>
-__global__ void __launch_bounds__(128, 1)
+// SOLVE = false: factorisation only (the solve of gbla_sgels_batched_ws runs
+// in k_ls_solve); F (nullable) receives the factors instead of A.
+template <typename T, int R, bool SOLVE = true>
+__global__ void __launch_bounds__(128, SOLVE ? 1 : 3)
     k_qr_warp(int m, int n, int nrhs, T *__restrict__ A, int64_t sA, T *__restrict__ B, int64_t sB,
-              T *__restrict__ tau_g, int64_t sTau, int *__restrict__ info, int flags, int refine, int batch) {
+              T *__restrict__ tau_g, int64_t sTau, int *__restrict__ info, int flags, int refine, int batch,
+              T *__restrict__ F = nullptr, int64_t sF = 0) {
     extern __shared__ __align__(16) unsigned char qsm_raw[];
     T *qsm = reinterpret_cast<T *>(qsm_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -316,7 +319,7 @@ __global__ void __launch_bounds__(128, 1)
     int fail = q.factor(m, n, tau_s);
     if (info && lane == 0) info[mat] = fail;
 
-    if ((flags & QR_SOLVE) && nrhs > 0) {
+    if (SOLVE && (flags & QR_SOLVE) && nrhs > 0) {
         T *b_g = B + mat * sB;
         for (int c = 0; c < nrhs; c++) {
             T y[R], b[R];
@@ -329,7 +332,7 @@ __global__ void __launch_bounds__(128, 1)
             q.apply_qt(n, tau_s, y);
             T x = q.back_solve(n, lane < n ? y[0] : T(0));
             if constexpr (kRefinable) {
-                if (refine > 0) x = refine_ls<R>(q, A0, m, n, b, x, tau_s, refine);
+                if (refine > 0) x = refine_ls<R>(q, A0, LDM, m, n, b, x, tau_s, refine);
             }
             // rows < n: solution (row r = this lane when t = 0, since n <= 32);
             // rows >= n: (Q^T b)(n:m), as gels leaves them
@@ -341,15 +344,126 @@ __global__ void __launch_bounds__(128, 1)
         }
     }
     if (flags & QR_WRITE_FACTORS) {
+        T *f_g = F ? F + mat * sF : a_g;
 #pragma unroll
         for (int j = 0; j < 32; j++)
 #pragma unroll
             for (int t = 0; t < R; t++) {
                 int r = lane + 32 * t;
-                if (j < n && r < m) a_g[(int64_t)j * m + r] = q.a[t][j];
+                if (j < n && r < m) f_g[(int64_t)j * m + r] = q.a[t][j];
             }
     }
     if ((flags & QR_WRITE_TAU) && tau_g && lane < n) tau_g[mat * sTau + lane] = tau_s[lane];
+}
+
+// ------------------------------------------ solve from stored factors
+// The QrWarp interface over factors held in shared memory (column-major,
+// 32 R padded rows): the same values and the same operation order as the
+// register-resident version, so both give bit-identical solutions.
+template <int R>
+struct QrSmem {
+    const float *Q;  // Q[j * 32 R + i] = factor element (i, j)
+    float dinv;
+    int lane;
+
+    __device__ __forceinline__ int row(int t) const { return lane + 32 * t; }
+    __device__ __forceinline__ float at(int t, int k) const { return Q[k * 32 * R + row(t)]; }
+
+    __device__ __forceinline__ void apply_h(int k, float tau, float (&y)[R]) const {
+        float s = 0.f;
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            float v = row(t) > k ? at(t, k) : (row(t) == k ? 1.f : 0.f);
+            s = fmaf(v, y[t], s);
+        }
+        s = tau * warp_sum(s);
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            float v = row(t) > k ? at(t, k) : (row(t) == k ? 1.f : 0.f);
+            y[t] = fmaf(-s, v, y[t]);
+        }
+    }
+    __device__ __forceinline__ void apply_qt(int n, const float *tau_s, float (&y)[R]) const {
+        for (int k = 0; k < n; k++) apply_h(k, tau_s[k], y);
+    }
+    __device__ __forceinline__ void apply_q(int n, const float *tau_s, float (&y)[R]) const {
+        for (int k = n - 1; k >= 0; k--) apply_h(k, tau_s[k], y);
+    }
+    __device__ __forceinline__ float back_solve(int n, float y) const {
+        float z = 0.f;
+        for (int j = n - 1; j >= 0; j--) {
+            float zj = shfl(y * dinv, j);
+            if (lane == j) z = zj;
+            if (lane < j) y = fmaf(-at(0, j), zj, y);
+        }
+        return z;
+    }
+    __device__ __forceinline__ float forward_solve_rt(int n, float g) const {
+        float h = 0.f;
+        for (int j = 0; j < n; j++) {
+            float part = lane < j ? at(0, j) * h : 0.f;
+            float sm = warp_sum(part);
+            float hj = shfl((g - sm) * dinv, j);
+            if (lane == j) h = hj;
+        }
+        return h;
+    }
+};
+
+// One block of 4 warps per least-squares system: factors and taus from the
+// workspace in shared memory, one warp per right-hand side (FP32 solve plus
+// double-FP32 refinement against the original A, still in A), then the
+// factors are copied into A as gels leaves them.
+template <int R>
+__global__ void __launch_bounds__(128)
+    k_ls_solve(int m, int n, int nrhs, float *__restrict__ A, int64_t sA, const float *__restrict__ F,
+               const float *__restrict__ tau_g, float *__restrict__ B, int64_t sB, int refine, int batch) {
+    extern __shared__ __align__(16) float lsm[];
+    constexpr int LDM = 32 * R;
+    float *Q = lsm;             // n columns x LDM
+    float *taus = Q + 32 * LDM;  // 32
+    const int64_t mat = blockIdx.x;
+    if (mat >= batch) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const float *f = F + mat * (int64_t)m * n;
+    for (int e = tid; e < n * LDM; e += 128) {
+        const int j = e / LDM, i = e % LDM;
+        Q[j * LDM + i] = i < m ? f[(int64_t)j * m + i] : 0.f;
+    }
+    if (tid < 32) taus[tid] = tid < n ? tau_g[mat * 32 + tid] : 0.f;
+    __syncthreads();
+    QrSmem<R> q;
+    q.Q = Q;
+    q.lane = lane;
+    {
+        const float d = lane < n ? Q[lane * LDM + lane] : 0.f;
+        q.dinv = (lane < n && d != 0.f) ? 1.f / d : 0.f;
+    }
+    const float *a_g = A + mat * sA;
+    float *b_g = B + mat * sB;
+    for (int c = warp; c < nrhs; c += 4) {
+        float y[R], b[R];
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            int r = lane + 32 * t;
+            b[t] = r < m ? b_g[(int64_t)c * m + r] : 0.f;
+            y[t] = b[t];
+        }
+        q.apply_qt(n, taus, y);
+        float x = q.back_solve(n, lane < n ? y[0] : 0.f);
+        if (refine > 0) x = refine_ls<R>(q, a_g, m, m, n, b, x, taus, refine);
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            int r = lane + 32 * t;
+            if (r < m) b_g[(int64_t)c * m + r] = r < n ? x : y[t];
+        }
+    }
+    __syncthreads();  // every warp is done with the original A
+    float *aw = A + mat * sA;
+    for (int e = tid; e < n * m; e += 128) {
+        const int j = e / m, i = e % m;
+        aw[(int64_t)j * m + i] = Q[j * LDM + i];
+    }
 }
 
 // --------------------------------------------- standalone ormqr / trsm
@@ -437,7 +551,8 @@ static gbla_status qr_launch(int m, int n, int nrhs, T *A, int64_t sA, T *B, int
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return from_cuda(e);
         }
-        kern<<<grid, 128, smem, st>>>(m, n, nrhs, A, sA, B, sB, tau, sTau, info, flags, refine, batch);
+        kern<<<grid, 128, smem, st>>>(m, n, nrhs, A, sA, B, sB, tau, sTau, info, flags, refine, batch,
+                                      (T *)nullptr, (int64_t)0);
         return launch_status();
     };
     switch (R) {
@@ -445,6 +560,45 @@ static gbla_status qr_launch(int m, int n, int nrhs, T *A, int64_t sA, T *B, int
         case 2: return go(k_qr_warp<T, 2>);
         case 3: return go(k_qr_warp<T, 3>);
         default: return go(k_qr_warp<T, 4>);
+    }
+}
+
+// workspace of gbla_sgels_batched_ws: factors (batch x m x n) + taus (batch x 32)
+static size_t gels_ws_bytes(int m, int n, int batch) {
+    if (m < 0 || n < 0 || batch < 0) return 0;
+    return sizeof(float) * ((size_t)batch * m * n + (size_t)batch * 32) + 256;
+}
+
+static gbla_status gels_ws_launch(int m, int n, int nrhs, float *A, int64_t sA, float *B, int64_t sB, int *info,
+                                  int refine, void *ws, size_t ws_bytes, int batch, cudaStream_t st) {
+    if (m < 0 || n < 0 || nrhs < 0 || batch < 0 || refine < 0 || m < n) return GBLA_INVALID_VALUE;
+    if (batch == 0 || n == 0) return GBLA_SUCCESS;
+    if (!A || sA < (int64_t)m * n || (nrhs > 0 && (!B || sB < (int64_t)m * nrhs))) return GBLA_INVALID_VALUE;
+    if (m > 128 || n > 32) return GBLA_NOT_SUPPORTED;
+    if (!ws || ws_bytes < gels_ws_bytes(m, n, batch)) return GBLA_WORKSPACE_TOO_SMALL;
+    float *F = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(ws) + 15) & ~uintptr_t(15));
+    float *tau = F + (size_t)batch * m * n;
+    const int R = (m + 31) / 32;
+    const unsigned g1 = (unsigned)((batch + 3) / 4);
+    const size_t smem1 = (size_t)4 * 32 * sizeof(float);
+    const size_t smem2 = sizeof(float) * ((size_t)32 * 32 * R + 32);
+    auto go = [&](auto kf, auto ks) -> gbla_status {
+        kf<<<g1, 128, smem1, st>>>(m, n, 0, A, sA, nullptr, 0, tau, 32, info, QR_WRITE_FACTORS | QR_WRITE_TAU, 0,
+                                   batch, F, (int64_t)m * n);
+        gbla_status s = launch_status();
+        if (s != GBLA_SUCCESS) return s;
+        if (smem2 > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+            if (e != cudaSuccess) return from_cuda(e);
+        }
+        ks<<<(unsigned)batch, 128, smem2, st>>>(m, n, nrhs, A, sA, F, tau, B, sB, refine, batch);
+        return launch_status();
+    };
+    switch (R) {
+        case 1: return go(k_qr_warp<float, 1, false>, k_ls_solve<1>);
+        case 2: return go(k_qr_warp<float, 2, false>, k_ls_solve<2>);
+        case 3: return go(k_qr_warp<float, 3, false>, k_ls_solve<3>);
+        default: return go(k_qr_warp<float, 4, false>, k_ls_solve<4>);
     }
 }
 
@@ -491,6 +645,12 @@ GBLA_API gbla_status gbla_dgeqrf_batched(int m, int n, double *A, int64_t sA, do
 GBLA_API gbla_status gbla_sgels_batched(int m, int n, int nrhs, float *A, int64_t sA, float *B, int64_t sB, int *info,
                                         int refine, int batch, cudaStream_t st) {
     return qr_launch<float>(m, n, nrhs, A, sA, B, sB, nullptr, 0, info, QR_WRITE_FACTORS | QR_SOLVE, refine, batch, st);
+}
+GBLA_API size_t gbla_sgels_batched_workspace_bytes(int m, int n, int batch) { return gels_ws_bytes(m, n, batch); }
+GBLA_API gbla_status gbla_sgels_batched_ws(int m, int n, int nrhs, float *A, int64_t sA, float *B, int64_t sB,
+                                           int *info, int refine, void *workspace, size_t workspace_bytes, int batch,
+                                           cudaStream_t st) {
+    return gels_ws_launch(m, n, nrhs, A, sA, B, sB, info, refine, workspace, workspace_bytes, batch, st);
 }
 GBLA_API gbla_status gbla_dgels_batched(int m, int n, int nrhs, double *A, int64_t sA, double *B, int64_t sB,
                                         int *info, int batch, cudaStream_t st) {

@@ -194,6 +194,17 @@ gbla_status gbla_sgels_batched(int m, int n, int nrhs, float *A, int64_t strideA
                                int *info, int refine_iters, int batch, cudaStream_t stream);
 gbla_status gbla_dgels_batched(int m, int n, int nrhs, double *A, int64_t strideA, double *B, int64_t strideB,
                                int *info, int batch, cudaStream_t stream);
+/* The same least squares in two kernels with a workspace: a register-resident
+ * factorisation writes the factors and taus to the workspace (the original A
+ * stays in place for the refinement residuals), then one block per system
+ * solves and refines its right-hand sides with one warp each from the factors
+ * in shared memory and finally copies the factors into A.  Results are
+ * bit-identical to gbla_sgels_batched.  workspace: at least
+ * gbla_sgels_batched_workspace_bytes(m, n, batch) bytes of device memory. */
+size_t gbla_sgels_batched_workspace_bytes(int m, int n, int batch);
+gbla_status gbla_sgels_batched_ws(int m, int n, int nrhs, float *A, int64_t strideA, float *B, int64_t strideB,
+                                  int *info, int refine_iters, void *workspace, size_t workspace_bytes, int batch,
+                                  cudaStream_t stream);
 
 /* ------------------------------------------------------------------- SVD */
 /* One-sided (Hestenes) Jacobi SVD A_i = U_i diag(S_i) Vt_i of m x n matrices

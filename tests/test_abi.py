@@ -48,6 +48,14 @@ def test_invalid_arguments_are_rejected_host_side(gbla_lib):
     assert L.gbla_scopy_rows(3, 2, 2, 2, fake, fake, None) == INVALID        # rows out of range
     assert L.gbla_saxpy(-1, 1.0, fake, fake, None) == INVALID
     assert L.gbla_sdot(4, fake, None, fake, fake, None) == INVALID
+    # two-kernel least squares: workspace size, m < n, and a workspace that is too small
+    ws = L.gbla_sgels_batched_workspace_bytes(128, 32, 8192)
+    assert ws >= 4 * (8192 * 128 * 32 + 8192 * 32)
+    assert L.gbla_sgels_batched_workspace_bytes(-1, 32, 8) == 0
+    assert L.gbla_sgels_batched_ws(4, 5, 1, fake, 20, fake, 4, None, 1, fake, 1 << 20, 1, None) == INVALID
+    assert L.gbla_sgels_batched_ws(8, 4, 1, fake, 32, fake, 8, None, 1, fake, 64, 2, None) == 4
+    assert L.gbla_sgels_batched_ws(8, 4, 1, fake, 32, fake, 8, None, 1, None, 1 << 20, 2, None) == 4
+    assert L.gbla_sgels_batched_ws(130, 4, 1, fake, 520, fake, 130, None, 1, fake, 1 << 20, 2, None) == 2
 
 
 def test_empty_problems_are_noops(gbla_lib):
@@ -57,6 +65,7 @@ def test_empty_problems_are_noops(gbla_lib):
     assert L.gbla_sgemm_batched(0, 3, 3, 1.0, None, 0, None, 0, 0.0, None, 0, 3, 0, None) == 0
     assert L.gbla_saxpy(0, 1.0, None, None, None) == 0
     assert L.gbla_stranspose_batched(0, 5, None, 0, None, 0, 3, None) == 0
+    assert L.gbla_sgels_batched_ws(8, 4, 1, None, 32, None, 8, None, 1, None, 0, 0, None) == 0
 
 
 @pytest.mark.parametrize("name", ["gbla_spotrf_batched", "gbla_sgemm_batched", "gbla_sdot"])

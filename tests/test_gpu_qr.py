@@ -13,13 +13,18 @@ TOL = {np.float32: G["precision_low"], np.float64: G["precision_high"]}
 PFX = {np.float32: "s", np.float64: "d"}
 
 
-def _gels(lib, A, B, dt, refine=0):
+def _gels(lib, A, B, dt, refine=0, workspace=False):
     import torch
     k, m, n = A.shape
     nrhs = B.shape[2]
     Ad, Bd = to_dev(A, dt), to_dev(B, dt)
     info = torch.full((k,), -1, dtype=torch.int32, device="cuda")
-    if dt == np.float32:
+    if dt == np.float32 and workspace:
+        wsb = lib.gbla_sgels_batched_workspace_bytes(m, n, k)
+        ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+        st = lib.gbla_sgels_batched_ws(m, n, nrhs, ptr(Ad), m * n, ptr(Bd), m * nrhs, ptr(info), refine, ptr(ws),
+                                       wsb, k, stream())
+    elif dt == np.float32:
         st = lib.gbla_sgels_batched(m, n, nrhs, ptr(Ad), m * n, ptr(Bd), m * nrhs, ptr(info), refine, k, stream())
     else:
         st = lib.gbla_dgels_batched(m, n, nrhs, ptr(Ad), m * n, ptr(Bd), m * nrhs, ptr(info), k, stream())
@@ -119,3 +124,34 @@ def test_d2b_config_full_size(gbla_lib, cuda):
     idx = np.arange(0, k, 97)
     _, Xo = O.gels(A[idx], B[idx])
     assert rel_err(x[idx], Xo[:, :n]) < 1e-6
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (20, 3), (33, 32), (64, 17), (97, 31), (100, 32), (128, 32)])
+@pytest.mark.parametrize("refine", [0, 1, 2])
+@pytest.mark.parametrize("nrhs", [1, 4, 7])
+def test_gels_workspace_path_is_bit_identical(gbla_lib, cuda, shape, refine, nrhs):
+    """gbla_sgels_batched_ws (factor kernel + one-block-per-system solve)
+    returns exactly the factors, solutions and info of gbla_sgels_batched."""
+    m, n = shape
+    A, B = workloads.d2b_least_squares(k=37, m=m, n=n, nrhs=nrhs, cond=1e3, seed=m * 7 + n)
+    F1, X1, i1 = _gels(gbla_lib, A, B, np.float32, refine=refine)
+    F2, X2, i2 = _gels(gbla_lib, A, B, np.float32, refine=refine, workspace=True)
+    assert (i1 == i2).all() and (i1 == 0).all()
+    assert np.array_equal(F1, F2)
+    assert np.array_equal(X1, X2)
+
+
+def test_gels_workspace_rank_deficient_and_too_small(gbla_lib, cuda):
+    import torch
+    A = np.zeros((2, 6, 3), np.float32)
+    A[0] = np.random.default_rng(0).standard_normal((6, 3))
+    A[1, :, 0] = 1.0
+    F1, X1, i1 = _gels(gbla_lib, A, np.ones((2, 6, 2)), np.float32, refine=1)
+    F2, X2, i2 = _gels(gbla_lib, A, np.ones((2, 6, 2)), np.float32, refine=1, workspace=True)
+    assert (i1 == i2).all() and i2[0] == 0 and i2[1] in (2, 3)
+    assert np.array_equal(F1, F2) and np.array_equal(X1, X2, equal_nan=True)
+    Ad, Bd = to_dev(A, np.float32), to_dev(np.ones((2, 6, 1)), np.float32)
+    wsb = gbla_lib.gbla_sgels_batched_workspace_bytes(6, 3, 2)
+    ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+    assert gbla_lib.gbla_sgels_batched_ws(6, 3, 1, ptr(Ad), 18, ptr(Bd), 6, None, 1, ptr(ws), wsb - 1, 2,
+                                          stream()) == 4
