@@ -444,20 +444,22 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
         torch.from_numpy(np.ascontiguousarray(LB.transpose(0, 2, 1))).pin_memory()
     hC = torch.empty_like(hA).pin_memory()
     hX = torch.empty_like(hLB).pin_memory()
-    dLA, dLB = torch.empty_like(LA0), torch.empty_like(LB0)
+    # host-buffer calls: chunks rotate over three worker streams, so copies in,
+    # kernels and copies out of consecutive chunks overlap
+    pipe = C.c_void_p()
+    _lib.check(L.gbla_pipeline_create(3, C.byref(pipe)), "pipeline")
 
     def e2e_step():
-        Ag.copy_(hA, non_blocking=True); Bg.copy_(hB, non_blocking=True)
-        dLA.copy_(hLA, non_blocking=True); dLB.copy_(hLB, non_blocking=True)
-        _lib.check(L.gbla_sgemm_batched(64, 64, 64, 1.0, Ag.data_ptr(), 4096, Bg.data_ptr(), 4096, 0.0,
-                                        Cg.data_ptr(), 4096, kg, 0, st), "sgemm")
-        _lib.check(L.gbla_sgels_batched_ws(m, n, r, dLA.data_ptr(), m * n, dLB.data_ptr(), m * r, info.data_ptr(),
-                                           args.refine, ws.data_ptr(), ws_bytes, kl, st), "sgels")
-        hC.copy_(Cg, non_blocking=True); hX.copy_(dLB, non_blocking=True)
+        _lib.check(L.gbla_sgemm_batched_host(pipe, 64, 64, 64, 1.0, hA.data_ptr(), 4096, hB.data_ptr(), 4096, 0.0,
+                                             hC.data_ptr(), 4096, kg, 0, 0, st), "sgemm_host")
+        _lib.check(L.gbla_sgels_batched_host(pipe, m, n, r, hLA.data_ptr(), m * n, None, hLB.data_ptr(), m * r,
+                                             hX.data_ptr(), None, args.refine, kl, 0, st), "sgels_host")
 
     for _ in range(2):
         e2e_step()
     torch.cuda.synchronize()
+    # the host results agree with the device-resident path
+    e2e_ok = bool(torch.equal(hX, LBs[0].cpu())) and bool(torch.equal(hC, Cg.cpu()))
     esteps = max(3, min(args.steps, 10))
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record()
@@ -469,6 +471,7 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
     e2e_max, _ = aggregate(e2e_t, 0.0, world, dist, dev)
     h2d = (hA.numel() + hB.numel() + hLA.numel() + hLB.numel()) * 4
     d2h = (hC.numel() + hX.numel()) * 4
+    _lib.check(L.gbla_pipeline_destroy(pipe), "pipeline destroy")
 
     # ---- reference library path (cuBLAS / cuSOLVER calls of tensor.cuh) on the same GPU
     reflib = None
@@ -500,9 +503,10 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
         "info_all_zero": info_ok,
         "e2e": {"value": (kg + kl) * world / e2e_max, "unit": "matrices/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_max * 1e3,
-                "path": "C ABI (gbla_sgemm_batched + gbla_sgels_batched_ws) with pinned host buffers, "
-                        "H2D of A, B, A_ls, B_ls and D2H of C, X inside the timed region"},
-        "gpu_launches": 3 * args.steps,  # GEMM + least-squares factorisation + solve
+                "path": "C ABI host-buffer calls (gbla_sgemm_batched_host + gbla_sgels_batched_host, chunks "
+                        "over 3 streams) on pinned host buffers: H2D of A, B, A_ls, B_ls and D2H of C, X inside "
+                        "the timed region", "matches_device_path": e2e_ok},
+        "gpu_launches": 3 * args.steps,  # device-resident step: GEMM + least-squares factorisation + solve
         "clocks": clk.summary(),
         "reference_library": reflib,
     }

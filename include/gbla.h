@@ -12,7 +12,9 @@
  * Conventions
  *  - Matrices are column-major with leading dimension = number of rows.
  *  - All calls are asynchronous on the given stream and allocate nothing;
- *    reductions that need scratch take a caller-provided workspace.
+ *    reductions that need scratch take a caller-provided workspace.  The
+ *    exceptions are objects made at set-up time (ragged plans, stream
+ *    pipelines, the warm-start network), which own their device memory.
  *  - Errors are returned as gbla_status; nothing is thrown or printed and the
  *    process is never terminated.  Numerical failures are reported per matrix
  *    through device `info` arrays with cuSOLVER's meaning (0 = success).
@@ -205,6 +207,36 @@ size_t gbla_sgels_batched_workspace_bytes(int m, int n, int batch);
 gbla_status gbla_sgels_batched_ws(int m, int n, int nrhs, float *A, int64_t strideA, float *B, int64_t strideB,
                                   int *info, int refine_iters, void *workspace, size_t workspace_bytes, int batch,
                                   cudaStream_t stream);
+
+/* ------------------------------------------------------ host-buffer calls */
+/* A stream pipeline: `streams` worker streams (1..8, 3 recommended) with
+ * their events and device staging buffers (grow-only; allocated by the first
+ * call that needs them, so make that call outside stream capture).  The
+ * *_host calls below take HOST matrices (page-locked for the copies to be
+ * asynchronous), split the batch into chunks of `chunk` matrices (0: about
+ * an eighth of the batch, at least 1024) and rotate the chunks over the
+ * workers, so that copies in, kernels and copies out of consecutive chunks
+ * overlap.  The calls are ordered on `stream` like a kernel launch: host
+ * buffers must stay valid, and results are available, once `stream` has
+ * reached that point.  One pipeline serves one stream at a time.  Replaces
+ * the synchronous upload -> call -> download sequence of DTensor
+ * (include/tensor.cuh:875-884, 1129-1154) around addAB and
+ * leastSquaresBatched. */
+typedef struct gbla_stream_pipeline gbla_stream_pipeline;
+gbla_status gbla_pipeline_create(int streams, gbla_stream_pipeline **pipeline);
+gbla_status gbla_pipeline_destroy(gbla_stream_pipeline *pipeline);
+/* gbla_sgemm_batched on host A, B, C (C read only when beta != 0). */
+gbla_status gbla_sgemm_batched_host(gbla_stream_pipeline *pipeline, int m, int n, int k, float alpha,
+                                    const float *A, int64_t strideA, const float *B, int64_t strideB, float beta,
+                                    float *C, int64_t strideC, int batch, gbla_gemm_mode mode, int chunk,
+                                    cudaStream_t stream);
+/* gbla_sgels_batched_ws on host matrices: A and B are inputs; X (stride
+ * strideB, may equal B) receives what gbla_sgels_batched leaves in B (the
+ * solution in rows [0, n)); F (nullable, stride strideA, may equal A) the QR
+ * factors; info (nullable) the per-system status. */
+gbla_status gbla_sgels_batched_host(gbla_stream_pipeline *pipeline, int m, int n, int nrhs, const float *A,
+                                    int64_t strideA, float *F, const float *B, int64_t strideB, float *X,
+                                    int *info, int refine_iters, int batch, int chunk, cudaStream_t stream);
 
 /* ------------------------------------------------------------------- SVD */
 /* One-sided (Hestenes) Jacobi SVD A_i = U_i diag(S_i) Vt_i of m x n matrices

@@ -56,6 +56,12 @@ def test_invalid_arguments_are_rejected_host_side(gbla_lib):
     assert L.gbla_sgels_batched_ws(8, 4, 1, fake, 32, fake, 8, None, 1, fake, 64, 2, None) == 4
     assert L.gbla_sgels_batched_ws(8, 4, 1, fake, 32, fake, 8, None, 1, None, 1 << 20, 2, None) == 4
     assert L.gbla_sgels_batched_ws(130, 4, 1, fake, 520, fake, 130, None, 1, fake, 1 << 20, 2, None) == 2
+    # host-buffer pipeline calls: no pipeline, bad stream counts
+    assert L.gbla_pipeline_create(0, C.byref(C.c_void_p())) == INVALID
+    assert L.gbla_pipeline_create(3, None) == INVALID
+    assert L.gbla_sgemm_batched_host(None, 4, 4, 4, 1.0, fake, 16, fake, 16, 0.0, fake, 16, 1, 0, 0, None) == INVALID
+    assert L.gbla_sgels_batched_host(None, 8, 4, 1, fake, 32, None, fake, 8, fake, None, 1, 1, 0, None) == INVALID
+    assert L.gbla_pipeline_destroy(None) == 0
 
 
 def test_empty_problems_are_noops(gbla_lib):
