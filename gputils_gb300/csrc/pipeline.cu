@@ -176,9 +176,8 @@ GBLA_API gbla_status gbla_sgels_batched_host(gbla_stream_pipeline *p, int m, int
     if (!A || sA < ea || (nrhs > 0 && (!B || !X || sB < eb))) return GBLA_INVALID_VALUE;
     if (m > 128 || n > 32) return GBLA_NOT_SUPPORTED;
     const int64_t cs = chunk > 0 ? (chunk < batch ? chunk : batch) : default_chunk(batch, 1024);
-    const size_t wsb = gbla_sgels_batched_workspace_bytes(m, n, (int)cs);
     const size_t ba = round_up(cs * ea * 4, 256), bb = round_up(cs * eb * 4, 256), bi = round_up(cs * 4, 256);
-    gbla_status s = reserve(p, ba + bb + bi + round_up((int64_t)wsb, 256) + 256);
+    gbla_status s = reserve(p, ba + bb + bi + 256);
     if (s == GBLA_SUCCESS) s = fork(p, st);
     const size_t W = p->workers.size();
     for (int64_t c0 = 0, i = 0; s == GBLA_SUCCESS && c0 < batch; c0 += cs, i++) {
@@ -187,12 +186,11 @@ GBLA_API gbla_status gbla_sgels_batched_host(gbla_stream_pipeline *p, int m, int
         char *base = align256(w.buf);
         float *dA = reinterpret_cast<float *>(base), *dB = reinterpret_cast<float *>(base + ba);
         int *dI = reinterpret_cast<int *>(base + ba + bb);
-        void *ws = base + ba + bb + bi;
         s = copy_matrices(dA, ea * 4, A + c0 * sA, sA * 4, ea * 4, cnt, cudaMemcpyHostToDevice, w.stream);
         if (s == GBLA_SUCCESS && nrhs > 0)
             s = copy_matrices(dB, eb * 4, B + c0 * sB, sB * 4, eb * 4, cnt, cudaMemcpyHostToDevice, w.stream);
         if (s == GBLA_SUCCESS)
-            s = gbla_sgels_batched_ws(m, n, nrhs, dA, ea, dB, eb, dI, refine, ws, wsb, (int)cnt, w.stream);
+            s = gbla_sgels_batched(m, n, nrhs, dA, ea, dB, eb, dI, refine, (int)cnt, w.stream);
         if (s == GBLA_SUCCESS && nrhs > 0)
             s = copy_matrices(X + c0 * sB, sB * 4, dB, eb * 4, eb * 4, cnt, cudaMemcpyDeviceToHost, w.stream);
         if (s == GBLA_SUCCESS && F)

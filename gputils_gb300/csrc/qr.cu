@@ -410,28 +410,26 @@ struct QrSmem {
     }
 };
 
-// One block of 4 warps per least-squares system: factors and taus from the
-// workspace in shared memory, one warp per right-hand side (FP32 solve plus
-// double-FP32 refinement against the original A, still in A), then the
-// factors are copied into A as gels leaves them.
+// 4-byte asynchronous global -> shared copy (zero-filled when `valid` is false;
+// the source address is then not read).
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Solve phase shared by k_ls_solve and k_gels_cta: factors (Q, column-major,
+// 32 R rows), taus and the original A (A0, refinement only) are in shared
+// memory; one warp per right-hand side solves in FP32 and refines with
+// double-FP32 residuals, then the block copies the factors into A.
 template <int R>
-__global__ void __launch_bounds__(128)
-    k_ls_solve(int m, int n, int nrhs, float *__restrict__ A, int64_t sA, const float *__restrict__ F,
-               const float *__restrict__ tau_g, float *__restrict__ B, int64_t sB, int refine, int batch) {
-    extern __shared__ __align__(16) float lsm[];
+__device__ __forceinline__ void ls_solve_block(int m, int n, int nrhs, const float *Q, const float *A0,
+                                               const float *taus, float *a_g, float *b_g, int refine, int warp,
+                                               int lane) {
     constexpr int LDM = 32 * R;
-    float *Q = lsm;             // n columns x LDM
-    float *taus = Q + 32 * LDM;  // 32
-    const int64_t mat = blockIdx.x;
-    if (mat >= batch) return;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const float *f = F + mat * (int64_t)m * n;
-    for (int e = tid; e < n * LDM; e += 128) {
-        const int j = e / LDM, i = e % LDM;
-        Q[j * LDM + i] = i < m ? f[(int64_t)j * m + i] : 0.f;
-    }
-    if (tid < 32) taus[tid] = tid < n ? tau_g[mat * 32 + tid] : 0.f;
-    __syncthreads();
     QrSmem<R> q;
     q.Q = Q;
     q.lane = lane;
@@ -439,8 +437,6 @@ __global__ void __launch_bounds__(128)
         const float d = lane < n ? Q[lane * LDM + lane] : 0.f;
         q.dinv = (lane < n && d != 0.f) ? 1.f / d : 0.f;
     }
-    const float *a_g = A + mat * sA;
-    float *b_g = B + mat * sB;
     for (int c = warp; c < nrhs; c += 4) {
         float y[R], b[R];
 #pragma unroll
@@ -451,19 +447,195 @@ __global__ void __launch_bounds__(128)
         }
         q.apply_qt(n, taus, y);
         float x = q.back_solve(n, lane < n ? y[0] : 0.f);
-        if (refine > 0) x = refine_ls<R>(q, a_g, m, m, n, b, x, taus, refine);
+        if (refine > 0) x = refine_ls<R>(q, A0, LDM, m, n, b, x, taus, refine);
 #pragma unroll
         for (int t = 0; t < R; t++) {
             int r = lane + 32 * t;
             if (r < m) b_g[(int64_t)c * m + r] = r < n ? x : y[t];
         }
     }
-    __syncthreads();  // every warp is done with the original A
-    float *aw = A + mat * sA;
-    for (int e = tid; e < n * m; e += 128) {
-        const int j = e / m, i = e % m;
-        aw[(int64_t)j * m + i] = Q[j * LDM + i];
+    // the factors into A (the original A is no longer read from global memory)
+    for (int j = warp; j < n; j += 4) {
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            const int i = lane + 32 * t;
+            if (i < m) a_g[(int64_t)j * m + i] = Q[j * LDM + i];
+        }
     }
+}
+
+// One block of 4 warps per least-squares system: the factors and taus (from
+// the workspace) and the original A (still in A) are staged in shared memory
+// with asynchronous copies, all in flight at once, then ls_solve_block.
+template <int R>
+__global__ void __launch_bounds__(128)
+    k_ls_solve(int m, int n, int nrhs, float *__restrict__ A, int64_t sA, const float *__restrict__ F,
+               const float *__restrict__ tau_g, float *__restrict__ B, int64_t sB, int refine, int batch) {
+    extern __shared__ __align__(16) float lsm[];
+    constexpr int LDM = 32 * R;
+    float *Q = lsm;                // n columns x LDM: factors
+    float *A0 = Q + 32 * LDM;      // n columns x LDM: original matrix (refinement only)
+    float *taus = A0 + (refine > 0 ? 32 * LDM : 0);  // 32
+    const int64_t mat = blockIdx.x;
+    if (mat >= batch) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const float *f = F + mat * (int64_t)m * n;
+    float *a_g = A + mat * sA;
+    for (int j = warp; j < n; j += 4) {
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            const int i = lane + 32 * t;
+            const bool ok = i < m;
+            cp_async4(Q + j * LDM + i, f + (ok ? (int64_t)j * m + i : 0), ok);
+            if (refine > 0) cp_async4(A0 + j * LDM + i, a_g + (ok ? (int64_t)j * m + i : 0), ok);
+        }
+    }
+    if (tid < 32) taus[tid] = tid < n ? tau_g[mat * 32 + tid] : 0.f;
+    cp_async_wait_all();
+    __syncthreads();
+    ls_solve_block<R>(m, n, nrhs, Q, A0, taus, a_g, B + mat * sB, refine, warp, lane);
+}
+
+// Total over the warp of 8 slots, reduce-scattered: on return lanes
+// 4 s .. 4 s + 3 hold the total of slot s.  The additions pair lanes in the
+// same order as reduce_scatter32 (bit 4 first), so a slot's total is the
+// same value either function computes.
+__device__ __forceinline__ float reduce_scatter8(const float (&p)[8], int lane) {
+    float q[4];
+    const bool b4 = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float mine = b4 ? p[i + 4] : p[i], other = b4 ? p[i] : p[i + 4];
+        q[i] = mine + shfl_xor(other, 16);
+    }
+    const bool b3 = lane & 8;
+    float r[2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const float mine = b3 ? q[i + 2] : q[i], other = b3 ? q[i] : q[i + 2];
+        r[i] = mine + shfl_xor(other, 8);
+    }
+    const bool b2 = lane & 4;
+    float s = (b2 ? r[1] : r[0]) + shfl_xor(b2 ? r[0] : r[1], 4);
+    s += shfl_xor(s, 2);
+    s += shfl_xor(s, 1);
+    return s;
+}
+
+// Least squares, one block of 4 warps per system, everything on chip.
+// Factorisation: warp w holds columns w, w + 4, ..., w + 28 (rows lane + 32 t
+// in registers, 8 R values per lane).  At step k the owner of column k
+// (warp k mod 4) forms the Householder vector exactly as QrWarp::factor does
+// and publishes it (explicit unit diagonal, double-buffered) in shared
+// memory; after one block barrier every warp applies the reflector to its
+// columns j > k.  The
+// per-lane partial dot products and the reduction tree are those of
+// QrWarp::factor, so factors, solutions and info are bit-identical to the
+// one-warp-per-system kernel.  Then the factors go to shared memory and
+// ls_solve_block solves one right-hand side per warp.
+template <int R>
+__global__ void __launch_bounds__(128)
+    k_gels_cta(int m, int n, int nrhs, float *__restrict__ A, int64_t sA, float *__restrict__ B, int64_t sB,
+               int *__restrict__ info, int refine, int batch) {
+    extern __shared__ __align__(16) float gsm[];
+    constexpr int LDM = 32 * R;
+    float *Q = gsm;                           // 32 columns x LDM: factors
+    float *vbuf = Q + 32 * LDM;               // 2 x LDM: Householder vector of the step (double-buffered)
+    float *taus = vbuf + 2 * LDM;             // 32
+    float *A0 = taus + 32;                    // 32 columns x LDM: original matrix (refinement only)
+    const int64_t mat = blockIdx.x;
+    if (mat >= batch) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float *a_g = A + mat * sA;
+    float a[R][8];  // column warp + 4 c, rows lane + 32 t
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const int j = warp + 4 * c;
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            const int r = lane + 32 * t;
+            const float v = (j < n && r < m) ? a_g[(int64_t)j * m + r] : 0.f;
+            a[t][c] = v;
+            if (refine > 0) A0[j * LDM + r] = v;
+        }
+    }
+    // Steps k = 4 kb + kk: the pivot column is slot kb of warp kk, so with kb
+    // unrolled every register index is a compile-time constant and a warp
+    // visits only its slots c >= kb (slot kb only while its column is > k).
+#pragma unroll
+    for (int kb = 0; kb < 8; kb++) {
+        for (int kk = 0; kk < 4; kk++) {
+            const int k = 4 * kb + kk;
+            if (k >= n) break;
+            float *vb = vbuf + (k & 1) * LDM;
+            if (warp == kk) {
+                float x2 = 0.f;
+#pragma unroll
+                for (int t = 0; t < R; t++) {
+                    const int r = lane + 32 * t;
+                    if (r > k && r < m) x2 = fmaf(a[t][kb], a[t][kb], x2);
+                }
+                x2 = warp_sum(x2);
+                const float alpha = shfl(a[0][kb], k);
+                float tau = 0.f;
+                if (x2 > 0.f) {
+                    const float beta = -copysignf(sqrtf(fmaf(alpha, alpha, x2)), alpha);
+                    tau = (beta - alpha) / beta;
+                    const float scal = 1.f / (alpha - beta);
+#pragma unroll
+                    for (int t = 0; t < R; t++)
+                        if (lane + 32 * t > k) a[t][kb] *= scal;
+                    if (lane == k) a[0][kb] = beta;
+                }
+#pragma unroll
+                for (int t = 0; t < R; t++) {
+                    const int r = lane + 32 * t;
+                    vb[r] = r > k ? a[t][kb] : (r == k ? 1.f : 0.f);
+                }
+                // tau != 0 exactly when x2 > 0 (then tau = 1 - alpha / beta is in [1, 2])
+                if (lane == 0) taus[k] = tau;
+            }
+            __syncthreads();
+            const float tau = taus[k];
+            if (tau != 0.f) {
+                float v[R];
+#pragma unroll
+                for (int t = 0; t < R; t++) v[t] = vb[lane + 32 * t];
+                const bool own_active = warp > kk;  // slot kb holds column warp + 4 kb > k
+                float p[8];
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    float sdot = 0.f;
+                    if (c > kb || (c == kb && own_active)) {
+#pragma unroll
+                        for (int t = 0; t < R; t++) sdot = fmaf(v[t], a[t][c], sdot);
+                    }
+                    p[c] = sdot;
+                }
+                const float w = reduce_scatter8(p, lane);
+#pragma unroll
+                for (int c = kb; c < 8; c++) {
+                    if ((c > kb || own_active) && warp + 4 * c < n) {
+                        const float twj = tau * shfl(w, 4 * c);
+#pragma unroll
+                        for (int t = 0; t < R; t++) a[t][c] = fmaf(-twj, v[t], a[t][c]);
+                    }
+                }
+            }
+        }
+    }
+    // factors to shared memory (all 32 columns: zeros beyond n)
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+#pragma unroll
+        for (int t = 0; t < R; t++) Q[(warp + 4 * c) * LDM + lane + 32 * t] = a[t][c];
+    __syncthreads();
+    if (warp == 0) {
+        // info: first k whose diagonal entry R_kk is exactly zero (1-based)
+        const unsigned zero = __ballot_sync(FULL, lane < n && Q[lane * LDM + lane] == 0.f);
+        if (info && lane == 0) info[mat] = zero ? __ffs(zero) : 0;
+    }
+    ls_solve_block<R>(m, n, nrhs, Q, A0, taus, a_g, B + mat * sB, refine, warp, lane);
 }
 
 // --------------------------------------------- standalone ormqr / trsm
@@ -563,6 +735,32 @@ static gbla_status qr_launch(int m, int n, int nrhs, T *A, int64_t sA, T *B, int
     }
 }
 
+// Single-precision least squares, one block per system (k_gels_cta).
+static gbla_status gels_cta_launch(int m, int n, int nrhs, float *A, int64_t sA, float *B, int64_t sB, int *info,
+                                   int refine, int batch, cudaStream_t st) {
+    if (m < 0 || n < 0 || nrhs < 0 || batch < 0 || refine < 0 || m < n) return GBLA_INVALID_VALUE;
+    if (batch == 0 || n == 0) return GBLA_SUCCESS;
+    if (!A || sA < (int64_t)m * n || (nrhs > 0 && (!B || sB < (int64_t)m * nrhs))) return GBLA_INVALID_VALUE;
+    if (m > 128 || n > 32) return GBLA_NOT_SUPPORTED;
+    const int R = (m + 31) / 32;
+    // factors, two Householder vectors, taus, and the original A when refining
+    const size_t smem = sizeof(float) * ((size_t)(refine > 0 ? 2 : 1) * 32 * 32 * R + 2 * 32 * R + 32);
+    auto go = [&](auto kern) -> gbla_status {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return from_cuda(e);
+        }
+        kern<<<(unsigned)batch, 128, smem, st>>>(m, n, nrhs, A, sA, B, sB, info, refine, batch);
+        return launch_status();
+    };
+    switch (R) {
+        case 1: return go(k_gels_cta<1>);
+        case 2: return go(k_gels_cta<2>);
+        case 3: return go(k_gels_cta<3>);
+        default: return go(k_gels_cta<4>);
+    }
+}
+
 // workspace of gbla_sgels_batched_ws: factors (batch x m x n) + taus (batch x 32)
 static size_t gels_ws_bytes(int m, int n, int batch) {
     if (m < 0 || n < 0 || batch < 0) return 0;
@@ -581,7 +779,7 @@ static gbla_status gels_ws_launch(int m, int n, int nrhs, float *A, int64_t sA, 
     const int R = (m + 31) / 32;
     const unsigned g1 = (unsigned)((batch + 3) / 4);
     const size_t smem1 = (size_t)4 * 32 * sizeof(float);
-    const size_t smem2 = sizeof(float) * ((size_t)32 * 32 * R + 32);
+    const size_t smem2 = sizeof(float) * ((size_t)(refine > 0 ? 2 : 1) * 32 * 32 * R + 32);
     auto go = [&](auto kf, auto ks) -> gbla_status {
         kf<<<g1, 128, smem1, st>>>(m, n, 0, A, sA, nullptr, 0, tau, 32, info, QR_WRITE_FACTORS | QR_WRITE_TAU, 0,
                                    batch, F, (int64_t)m * n);
@@ -644,7 +842,7 @@ GBLA_API gbla_status gbla_dgeqrf_batched(int m, int n, double *A, int64_t sA, do
 }
 GBLA_API gbla_status gbla_sgels_batched(int m, int n, int nrhs, float *A, int64_t sA, float *B, int64_t sB, int *info,
                                         int refine, int batch, cudaStream_t st) {
-    return qr_launch<float>(m, n, nrhs, A, sA, B, sB, nullptr, 0, info, QR_WRITE_FACTORS | QR_SOLVE, refine, batch, st);
+    return gels_cta_launch(m, n, nrhs, A, sA, B, sB, info, refine, batch, st);
 }
 GBLA_API size_t gbla_sgels_batched_workspace_bytes(int m, int n, int batch) { return gels_ws_bytes(m, n, batch); }
 GBLA_API gbla_status gbla_sgels_batched_ws(int m, int n, int nrhs, float *A, int64_t sA, float *B, int64_t sB,

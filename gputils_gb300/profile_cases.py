@@ -2,7 +2,7 @@
 
     python -m gputils_gb300.profile_cases ragged [--count 4000] [--dtype f32]
     python -m gputils_gb300.profile_cases svd64 [--count 4096] [--warm]
-    python -m gputils_gb300.profile_cases gels [--count 8192] [--single-kernel]
+    python -m gputils_gb300.profile_cases gels [--count 8192] [--two-kernel]
 
 Each case runs one call of the library on seeded inputs of the benchmark's
 distributions (a few hundred MB on the device at most), checks the status
@@ -79,7 +79,7 @@ def svd64(count: int, warm: bool, repeat: int) -> dict:
             "sweeps": float(sw.float().mean())}
 
 
-def gels(count: int, repeat: int, single: bool = False) -> dict:
+def gels(count: int, repeat: int, two_kernel: bool = False) -> dict:
     import torch
     L = _lib.lib()
     A, B = workloads.d2b_least_squares(k=count)
@@ -95,7 +95,7 @@ def gels(count: int, repeat: int, single: bool = False) -> dict:
         Ad, Bd = Ah.clone(), Bh.clone()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        if single:
+        if not two_kernel:
             _lib.check(L.gbla_sgels_batched(m, nn, r, Ad.data_ptr(), m * nn, Bd.data_ptr(), m * r, info.data_ptr(),
                                             1, k, _stream()), "sgels")
         else:
@@ -105,7 +105,7 @@ def gels(count: int, repeat: int, single: bool = False) -> dict:
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
     assert int(info.max()) == 0
-    return {"case": "gels", "systems": k, "single_kernel": single, "ms": min(times)}
+    return {"case": "gels", "systems": k, "two_kernel": two_kernel, "ms": min(times)}
 
 
 def main(argv=None):
@@ -118,14 +118,15 @@ def main(argv=None):
     ap.add_argument("--nmin", type=int, default=4, help="ragged: smallest n")
     ap.add_argument("--rhs-max", type=int, default=8, help="ragged: largest nrhs")
     ap.add_argument("--refine", type=int, default=-1, help="ragged: refinement steps (default 1 f32, 2 f64)")
-    ap.add_argument("--single-kernel", action="store_true", help="gels: the one-kernel entry point")
+    ap.add_argument("--two-kernel", action="store_true",
+                    help="gels: the workspace entry point (warp factorisation + block solve)")
     a = ap.parse_args(argv)
     if a.case == "ragged":
         out = ragged(a.count or 4000, a.dtype, a.repeat, a.nmin, a.rhs_max, a.refine)
     elif a.case == "svd64":
         out = svd64(a.count or 4096, a.warm, a.repeat)
     else:
-        out = gels(a.count or 8192, a.repeat, a.single_kernel)
+        out = gels(a.count or 8192, a.repeat, a.two_kernel)
     print(json.dumps(out), flush=True)
 
 

@@ -190,18 +190,22 @@ gbla_status gbla_dtrsm_upper_batched(int n, int nc, const double *R, int64_t ldr
  * of each B_i column with the solution (rows [n, m) hold (Q^T b)(n:m)).
  * Single precision: refine_iters steps of augmented-system refinement with
  * double-FP32 residuals recover FP64-level accuracy of x.  info as geqrf.
+ * Single precision runs one block of four warps per system, on chip from
+ * load to store (each warp factorises a quarter of the columns, then solves
+ * one right-hand side at a time); double precision one warp per system.
  * Replaces cublas<t>gelsBatched in DTensor::leastSquaresBatched
  * (include/tensor.cuh:1340-1394), which allows nrhs = 1 only. */
 gbla_status gbla_sgels_batched(int m, int n, int nrhs, float *A, int64_t strideA, float *B, int64_t strideB,
                                int *info, int refine_iters, int batch, cudaStream_t stream);
 gbla_status gbla_dgels_batched(int m, int n, int nrhs, double *A, int64_t strideA, double *B, int64_t strideB,
                                int *info, int batch, cudaStream_t stream);
-/* The same least squares in two kernels with a workspace: a register-resident
- * factorisation writes the factors and taus to the workspace (the original A
- * stays in place for the refinement residuals), then one block per system
- * solves and refines its right-hand sides with one warp each from the factors
- * in shared memory and finally copies the factors into A.  Results are
- * bit-identical to gbla_sgels_batched.  workspace: at least
+/* The same least squares on another schedule, in two kernels with a
+ * workspace: one warp per system factorises in registers and writes the
+ * factors and taus to the workspace (the original A stays in place for the
+ * refinement residuals), then one block per system solves and refines its
+ * right-hand sides with one warp each from the factors in shared memory and
+ * finally copies the factors into A.  Results are bit-identical to
+ * gbla_sgels_batched.  workspace: at least
  * gbla_sgels_batched_workspace_bytes(m, n, batch) bytes of device memory. */
 size_t gbla_sgels_batched_workspace_bytes(int m, int n, int batch);
 gbla_status gbla_sgels_batched_ws(int m, int n, int nrhs, float *A, int64_t strideA, float *B, int64_t strideB,
@@ -230,7 +234,7 @@ gbla_status gbla_sgemm_batched_host(gbla_stream_pipeline *pipeline, int m, int n
                                     const float *A, int64_t strideA, const float *B, int64_t strideB, float beta,
                                     float *C, int64_t strideC, int batch, gbla_gemm_mode mode, int chunk,
                                     cudaStream_t stream);
-/* gbla_sgels_batched_ws on host matrices: A and B are inputs; X (stride
+/* gbla_sgels_batched on host matrices: A and B are inputs; X (stride
  * strideB, may equal B) receives what gbla_sgels_batched leaves in B (the
  * solution in rows [0, n)); F (nullable, stride strideA, may equal A) the QR
  * factors; info (nullable) the per-system status. */

@@ -146,14 +146,10 @@ private:
             if (m_reduceWorkspace[i]) cudaFree(m_reduceWorkspace[i]);
             if (m_scalar[i]) cudaFree(m_scalar[i]);
         }
-        for (void *p : m_scratch)
-            if (p) cudaFree(p);
     }
 
     std::vector<cudaStream_t> m_streams;
     std::vector<void *> m_reduceWorkspace;
-    std::vector<void *> m_scratch;
-    std::vector<size_t> m_scratchBytes;
     std::vector<double *> m_scalar;
     size_t m_bytesAllocated = 0;
     size_t m_numStreams = 1;
@@ -172,20 +168,6 @@ public:
     void *reductionWorkspace(size_t idx = 0) {
         if (!m_reduceWorkspace[idx]) gpuErrChk(cudaMalloc(&m_reduceWorkspace[idx], gbla_reduce_workspace_bytes()));
         return m_reduceWorkspace[idx];
-    }
-
-    /** Grow-only scratch buffer of a stream (least-squares factors). */
-    void *scratch(size_t bytes, size_t idx = 0) {
-        if (m_scratch.size() < m_reduceWorkspace.size()) {
-            m_scratch.resize(m_reduceWorkspace.size(), nullptr);
-            m_scratchBytes.resize(m_reduceWorkspace.size(), 0);
-        }
-        if (m_scratchBytes[idx] < bytes) {
-            if (m_scratch[idx]) gpuErrChk(cudaFree(m_scratch[idx]));
-            gpuErrChk(cudaMalloc(&m_scratch[idx], bytes));
-            m_scratchBytes[idx] = bytes;
-        }
-        return m_scratch[idx];
     }
 
     /** One device scalar per stream for reduction results. */
@@ -277,11 +259,10 @@ inline gbla_status potrs(int n, int nrhs, const float *L, float *B, int batch, c
 inline gbla_status potrs(int n, int nrhs, const double *L, double *B, int batch, cudaStream_t st) {
     return gbla_dpotrs_batched(n, nrhs, L, (int64_t)n * n, B, (int64_t)n * nrhs, batch, st);
 }
-inline gbla_status gels(int m, int n, int nrhs, float *A, float *B, int batch, cudaStream_t st, void *ws,
-                        size_t wsb) {
-    return gbla_sgels_batched_ws(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, 1, ws, wsb, batch, st);
+inline gbla_status gels(int m, int n, int nrhs, float *A, float *B, int batch, cudaStream_t st) {
+    return gbla_sgels_batched(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, 1, batch, st);
 }
-inline gbla_status gels(int m, int n, int nrhs, double *A, double *B, int batch, cudaStream_t st, void *, size_t) {
+inline gbla_status gels(int m, int n, int nrhs, double *A, double *B, int batch, cudaStream_t st) {
     return gbla_dgels_batched(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, batch, st);
 }
 inline gbla_status geqrf(int m, int n, float *A, float *tau, int *info, cudaStream_t st) {
@@ -629,15 +610,8 @@ public:
         if (B.numCols() < 1) throw std::invalid_argument("[Least squares batched] rhs are not vectors");
         if (B.numMats() != m_numMats) throw std::invalid_argument("[Least squares batched] rhs numMats does not equal lhs numMats");
         if (m_numCols > m_numRows) throw std::invalid_argument("[Least squares batched] supports square or tall matrices only");
-        void *ws = nullptr;
-        size_t wsb = 0;
-        if constexpr (std::is_same_v<T, float>) {
-            // factors of the two-kernel solver (bit-identical to the one-kernel path)
-            wsb = gbla_sgels_batched_workspace_bytes((int)m_numRows, (int)m_numCols, (int)m_numMats);
-            ws = Session::getInstance().scratch(wsb, m_idxStream);
-        }
         gputils_detail::check(gputils_detail::gels((int)m_numRows, (int)m_numCols, (int)B.numCols(), raw(), B.raw(),
-                                                   (int)m_numMats, st(), ws, wsb),
+                                                   (int)m_numMats, st()),
                               "leastSquaresBatched");
     }
 
