@@ -192,8 +192,9 @@ struct QrWarp {
 };
 
 // Augmented-system refinement of one right-hand side (FP32 data, double-FP32
-// residuals).  A0: the original matrix, column stride lda; x0: FP32 solution
-// in lane j; returns the refined x in lane j.
+// residuals).  A0: the original matrix, column stride lda, rows [m, 32 R)
+// zero (every caller stages it zero-padded in shared memory); x0: FP32
+// solution in lane j; returns the refined x in lane j.
 template <int R, class QF>
 __device__ __forceinline__ float refine_ls(const QF &q, const float *A0, int lda, int m, int n,
                                            const float (&b)[R], float x0, const float *tau_s, int refine) {
@@ -220,7 +221,7 @@ __device__ __forceinline__ float refine_ls(const QF &q, const float *A0, int lda
 #pragma unroll
                 for (int t = 0; t < R; t++) {
                     int r = lane + 32 * t;
-                    float aij = r < m ? A0[(int64_t)j * lda + r] : 0.f;
+                    const float aij = A0[j * lda + r];
                     ff_fma(f[t], -aij, xjh, xjl);
                 }
             }
@@ -246,7 +247,7 @@ __device__ __forceinline__ float refine_ls(const QF &q, const float *A0, int lda
 #pragma unroll
                     for (int t = 0; t < R; t++) {
                         int r = lane + 32 * t;
-                        float aij = r < m ? A0[(int64_t)(j0 + c) * lda + r] : 0.f;
+                        const float aij = A0[(j0 + c) * lda + r];
                         ff_fma(acc[c], aij, rh[t], rl[t]);
                     }
                 }
@@ -369,19 +370,21 @@ struct QrSmem {
     __device__ __forceinline__ int row(int t) const { return lane + 32 * t; }
     __device__ __forceinline__ float at(int t, int k) const { return Q[k * 32 * R + row(t)]; }
 
+    // Reflector k < 32: rows 32 t (t >= 1) are all below the diagonal.
+    __device__ __forceinline__ float vk(int t, int k) const {
+        return t > 0 ? at(t, k) : (lane > k ? at(0, k) : (lane == k ? 1.f : 0.f));
+    }
     __device__ __forceinline__ void apply_h(int k, float tau, float (&y)[R]) const {
+        float v[R];
         float s = 0.f;
 #pragma unroll
         for (int t = 0; t < R; t++) {
-            float v = row(t) > k ? at(t, k) : (row(t) == k ? 1.f : 0.f);
-            s = fmaf(v, y[t], s);
+            v[t] = vk(t, k);
+            s = fmaf(v[t], y[t], s);
         }
         s = tau * warp_sum(s);
 #pragma unroll
-        for (int t = 0; t < R; t++) {
-            float v = row(t) > k ? at(t, k) : (row(t) == k ? 1.f : 0.f);
-            y[t] = fmaf(-s, v, y[t]);
-        }
+        for (int t = 0; t < R; t++) y[t] = fmaf(-s, v[t], y[t]);
     }
     __device__ __forceinline__ void apply_qt(int n, const float *tau_s, float (&y)[R]) const {
         for (int k = 0; k < n; k++) apply_h(k, tau_s[k], y);
