@@ -12,12 +12,14 @@
 // cost tensor time but no memory traffic).  This keeps the accumulator in the
 // plain M=128 layout: row r of D lives in TMEM lane r.
 //
-// Pipeline per block (256 threads, one pair-of-pairs at a time, 2 blocks/SM):
-//   all warps: global fp32 -> split -> shared memory (K-major core-matrix
-//   layout, no swizzle); fence.proxy.async; barrier; one thread issues the 24
-//   tcgen05.mma and commits to an mbarrier; all warps wait (bounded), read
-//   their TMEM rows with tcgen05.ld and store C.  Every wait is bounded; on a
-//   timeout the block records an error flag, frees its TMEM and exits.
+// Pipeline per block (256 threads, persistent, one block per SM):
+//   all warps: fp32 values in registers -> split -> shared memory (K-major
+//   core-matrix layout, no swizzle); fence.proxy.async; barrier; one thread
+//   issues the 24 tcgen05.mma and commits to an mbarrier; meanwhile every
+//   thread issues the global loads of its next pair-of-pairs (64 KB per SM in
+//   flight); all warps wait (bounded), read their TMEM rows with tcgen05.ld
+//   and store C.  Every wait is bounded; on a timeout the block records an
+//   error flag, frees its TMEM and exits.
 #include <cuda_bf16.h>
 #include "common.cuh"
 
@@ -106,7 +108,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 2)
+__global__ void __launch_bounds__(TC_THREADS, 1)
     k_gemm_tc_bf16x6(float alpha, const float *__restrict__ A, int64_t sA, const float *__restrict__ B, int64_t sB,
                      float beta, float *__restrict__ C, int64_t sC, int batch) {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -136,36 +138,48 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     uint32_t phase = 0;
 
     const int npp = (batch + 1) / 2;  // pair-of-pairs count
+    // Operand values of one pair-of-pairs, held in registers: A rows r in
+    // [0,128) are pair p0 + (r >= 64), row r & 63; B rows (N index) n in
+    // [0,128) are pair p0 + (n >= 64), column n & 63.  Each thread owns 4
+    // (row, kgroup) items of 8 K-consecutive values per operand.  The loads
+    // of the next pair-of-pairs are issued before waiting on the current
+    // MMA, so they stay in flight through the MMA and the epilogue.
+    float ra[4][8], rb[4][8];
+    auto load = [&](int qq) {
+        const int p0 = 2 * qq;
+#pragma unroll
+        for (int it = 0; it < 4; it++) {
+            const int item = tid + it * TC_THREADS;  // 0..1023 = 128 rows x 8 kgroups
+            const int row = item & 127, kg = item >> 7;
+            const int pr = p0 + (row >> 6);
+            const bool ok = pr < batch;
+            const float *a = A + (int64_t)(ok ? pr : p0) * sA;
+            const float *b = B + (int64_t)(ok ? pr : p0) * sB;
+            const int r = row & 63;
+#pragma unroll
+            for (int e = 0; e < 8; e++) ra[it][e] = ok ? a[(int64_t)(kg * 8 + e) * 64 + r] : 0.0f;
+            if (ok) {
+                const float4 *bp = reinterpret_cast<const float4 *>(b + (int64_t)r * 64 + kg * 8);
+                const float4 b0 = bp[0], b1 = bp[1];
+                rb[it][0] = b0.x; rb[it][1] = b0.y; rb[it][2] = b0.z; rb[it][3] = b0.w;
+                rb[it][4] = b1.x; rb[it][5] = b1.y; rb[it][6] = b1.z; rb[it][7] = b1.w;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; e++) rb[it][e] = 0.0f;
+            }
+        }
+    };
+    if ((int)blockIdx.x < npp) load(blockIdx.x);
     for (int q = blockIdx.x; q < npp; q += gridDim.x) {
         const int p0 = 2 * q;
         const bool has1 = p0 + 1 < batch;
-        // ---- load + split.  A rows: r in [0,128): pair p0 + (r >= 64), row r & 63.
-        //      B rows (N index): n in [0,128): pair p0 + (n >= 64), column n & 63.
-        // Each thread produces 8 core-matrix rows per operand: (row, kgroup) items.
-#pragma unroll 2
+        // ---- split the values in registers into the three BF16 operand tiles
+#pragma unroll
         for (int it = 0; it < 4; it++) {
-            int item = tid + it * TC_THREADS;  // 0..1023 = 128 rows x 8 kgroups
-            int row = item & 127, kg = item >> 7;
-            int pr = p0 + (row >> 6);
-            bool ok = pr < batch;
-            float va[8], vb[8];
-            const float *a = A + (int64_t)(ok ? pr : p0) * sA;
-            const float *b = B + (int64_t)(ok ? pr : p0) * sB;
-            int r = row & 63;
-#pragma unroll
-            for (int e = 0; e < 8; e++) va[e] = ok ? a[(int64_t)(kg * 8 + e) * 64 + r] : 0.0f;
-            if (ok) {
-                const float4 *bp = reinterpret_cast<const float4 *>(b + (int64_t)r * 64 + kg * 8);
-                float4 b0 = bp[0], b1 = bp[1];
-                vb[0] = b0.x; vb[1] = b0.y; vb[2] = b0.z; vb[3] = b0.w;
-                vb[4] = b1.x; vb[5] = b1.y; vb[6] = b1.z; vb[7] = b1.w;
-            } else {
-#pragma unroll
-                for (int e = 0; e < 8; e++) vb[e] = 0.0f;
-            }
-            uint32_t off = kmajor_off(row, kg);
-            store_split_row(sAop, off, va);
-            store_split_row(sBop, off, vb);
+            const int item = tid + it * TC_THREADS;
+            const uint32_t off = kmajor_off(item & 127, item >> 7);
+            store_split_row(sAop, off, ra[it]);
+            store_split_row(sBop, off, rb[it]);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -190,6 +204,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a)
                          : "memory");
         }
+        if (q + (int)gridDim.x < npp) load(q + gridDim.x);
         bool ok = mbar_wait(bar_a, phase);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) { atomicExch(&g_tc_error, 1); s_abort = 1; }
@@ -259,7 +274,7 @@ gbla_status tc_sgemm_bf16x6(int m, int n, int k, float alpha, const float *A, in
         attr_done[dev] = true;
     }
     int npp = (batch + 1) / 2;
-    int grid = sm_count() * 2;
+    int grid = sm_count();  // persistent: one block per SM, loads of the next pair-of-pairs overlap the current
     if (grid > npp) grid = npp;
     k_gemm_tc_bf16x6<<<grid, TC_THREADS, TC_SMEM, st>>>(alpha, A, sA, B, sB, beta, C, sC, batch);
     return launch_status();
