@@ -13,13 +13,14 @@
 // plain M=128 layout: row r of D lives in TMEM lane r.
 //
 // Pipeline per block (256 threads, persistent, one block per SM):
-//   all warps: fp32 values in registers -> split -> shared memory (K-major
-//   core-matrix layout, no swizzle); fence.proxy.async; barrier; one thread
-//   issues the 24 tcgen05.mma and commits to an mbarrier; meanwhile every
-//   thread issues the global loads of its next pair-of-pairs (64 KB per SM in
-//   flight); all warps wait (bounded), read their TMEM rows with tcgen05.ld
-//   and store C.  Every wait is bounded; on a timeout the block records an
-//   error flag, frees its TMEM and exits.
+//   cp.async copies raw fp32 operands into one of two shared-memory stages
+//   (64 KB each, one pair-of-pairs); all warps: raw stage -> split -> BF16
+//   operand tiles (K-major core-matrix layout, no swizzle); fence.proxy.async;
+//   barrier; the stage is refilled with the pair-of-pairs two steps ahead; one
+//   thread issues the 24 tcgen05.mma and commits to an mbarrier; all warps
+//   wait (bounded), read their TMEM rows with tcgen05.ld and store C.  Every
+//   wait is bounded; on a timeout the block records an error flag, waits for
+//   its copies, frees its TMEM and exits.
 #include <cuda_bf16.h>
 #include "common.cuh"
 
@@ -27,7 +28,9 @@ namespace gbla {
 
 constexpr int TC_THREADS = 256;
 constexpr int TC_TILE_BYTES = 128 * 64 * 2;    // one operand split: 128 rows x 64 K bf16 = 16 KB
-constexpr int TC_SMEM = 6 * TC_TILE_BYTES + 64; // A and B, 3 splits each, + barrier
+constexpr int TC_RAW_BYTES = 4 * 64 * 64 * 4;   // fp32 A_i, A_j, B_i, B_j of one pair-of-pairs = 64 KB
+// A and B, 3 splits each; two raw fp32 stages; barrier
+constexpr int TC_SMEM = 6 * TC_TILE_BYTES + 2 * TC_RAW_BYTES + 64;
 constexpr int TC_TMEM_COLS = 128;
 constexpr uint32_t TC_SPIN_LIMIT = 1u << 26;
 
@@ -114,7 +117,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sAop = smem;                      // 3 splits x 16 KB
     unsigned char *sBop = smem + 3 * TC_TILE_BYTES;  // 3 splits x 16 KB
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 6 * TC_TILE_BYTES);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 6 * TC_TILE_BYTES + 2 * TC_RAW_BYTES);
     __shared__ uint32_t s_tmem;
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -138,51 +141,76 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint32_t phase = 0;
 
     const int npp = (batch + 1) / 2;  // pair-of-pairs count
-    // Operand values of one pair-of-pairs, held in registers: A rows r in
-    // [0,128) are pair p0 + (r >= 64), row r & 63; B rows (N index) n in
-    // [0,128) are pair p0 + (n >= 64), column n & 63.  Each thread owns 4
-    // (row, kgroup) items of 8 K-consecutive values per operand.  The loads
-    // of the next pair-of-pairs are issued before waiting on the current
-    // MMA, so they stay in flight through the MMA and the epilogue.
-    float ra[4][8], rb[4][8];
-    auto load = [&](int qq) {
-        const int p0 = 2 * qq;
+    // Raw fp32 operands of one pair-of-pairs (stage layout: A_i, A_j, B_i, B_j,
+    // 16 KB each) are copied into shared memory with 16-byte cp.async, two
+    // stages deep, so the copies of pair-of-pairs q + 2 grid run while q is
+    // split, multiplied and stored.  A_p is column-major (element (r, k) at
+    // k * 64 + r) and kept linear: the split reads it down a column, lanes on
+    // consecutive rows.  B_p (element (k, n) at n * 64 + k) is read along k by
+    // lanes on consecutive n, so its 16-byte chunk kc of row n is stored at
+    // chunk position kc ^ (n & 7) of that row: eight consecutive rows then hit
+    // eight different bank groups.
+    unsigned char *raw0 = smem + 6 * TC_TILE_BYTES;
+    auto issue_raw = [&](int qq, int stage) {
+        if (qq < npp) {
+            unsigned char *dst0 = raw0 + stage * TC_RAW_BYTES;
 #pragma unroll
-        for (int it = 0; it < 4; it++) {
-            const int item = tid + it * TC_THREADS;  // 0..1023 = 128 rows x 8 kgroups
-            const int row = item & 127, kg = item >> 7;
-            const int pr = p0 + (row >> 6);
-            const bool ok = pr < batch;
-            const float *a = A + (int64_t)(ok ? pr : p0) * sA;
-            const float *b = B + (int64_t)(ok ? pr : p0) * sB;
-            const int r = row & 63;
-#pragma unroll
-            for (int e = 0; e < 8; e++) ra[it][e] = ok ? a[(int64_t)(kg * 8 + e) * 64 + r] : 0.0f;
-            if (ok) {
-                const float4 *bp = reinterpret_cast<const float4 *>(b + (int64_t)r * 64 + kg * 8);
-                const float4 b0 = bp[0], b1 = bp[1];
-                rb[it][0] = b0.x; rb[it][1] = b0.y; rb[it][2] = b0.z; rb[it][3] = b0.w;
-                rb[it][4] = b1.x; rb[it][5] = b1.y; rb[it][6] = b1.z; rb[it][7] = b1.w;
-            } else {
-#pragma unroll
-                for (int e = 0; e < 8; e++) rb[it][e] = 0.0f;
+            for (int u = 0; u < 16; u++) {
+                const int idx = (u & 7) * TC_THREADS + tid;  // 0..2047 within the operand
+                const int half = idx >> 10, c = idx & 1023;  // pair 2 qq + half, chunk c
+                const int pr = 2 * qq + half;
+                const bool ok = pr < batch;
+                const float *src;
+                uint32_t doff;
+                if (u < 8) {
+                    src = A + (int64_t)(ok ? pr : 0) * sA + c * 4;
+                    doff = (uint32_t)(half * 16384 + c * 16);
+                } else {
+                    const int n = c >> 4, kc = c & 15;
+                    src = B + (int64_t)(ok ? pr : 0) * sB + c * 4;
+                    doff = (uint32_t)(32768 + half * 16384 + n * 256 + ((kc ^ (n & 7)) << 4));
+                }
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst0 + doff)),
+                             "l"(src), "r"(ok ? 16 : 0)
+                             : "memory");
             }
         }
+        asm volatile("cp.async.commit_group;" ::: "memory");  // (possibly empty) group per call
     };
-    if ((int)blockIdx.x < npp) load(blockIdx.x);
-    for (int q = blockIdx.x; q < npp; q += gridDim.x) {
+    issue_raw(blockIdx.x, 0);
+    issue_raw(blockIdx.x + gridDim.x, 1);
+    int stage = 0;
+    for (int q = blockIdx.x; q < npp; q += gridDim.x, stage ^= 1) {
         const int p0 = 2 * q;
         const bool has1 = p0 + 1 < batch;
-        // ---- split the values in registers into the three BF16 operand tiles
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // this stage landed; the other may be in flight
+        __syncthreads();
+        // ---- split: raw fp32 (shared) -> three BF16 K-major operand tiles
+        {
+            const unsigned char *rs = raw0 + stage * TC_RAW_BYTES;
 #pragma unroll
-        for (int it = 0; it < 4; it++) {
-            const int item = tid + it * TC_THREADS;
-            const uint32_t off = kmajor_off(item & 127, item >> 7);
-            store_split_row(sAop, off, ra[it]);
-            store_split_row(sBop, off, rb[it]);
+            for (int it = 0; it < 4; it++) {
+                const int item = tid + it * TC_THREADS;  // 0..1023 = 128 rows x 8 kgroups
+                const int row = item & 127, kg = item >> 7;
+                const int half = row >> 6, r = row & 63;
+                const float *ra = reinterpret_cast<const float *>(rs + half * 16384);
+                float va[8], vb[8];
+#pragma unroll
+                for (int e = 0; e < 8; e++) va[e] = ra[(kg * 8 + e) * 64 + r];
+                const unsigned char *rb = rs + 32768 + half * 16384 + r * 256;
+                const float4 b0 = *reinterpret_cast<const float4 *>(rb + (((2 * kg) ^ (r & 7)) << 4));
+                const float4 b1 = *reinterpret_cast<const float4 *>(rb + (((2 * kg + 1) ^ (r & 7)) << 4));
+                vb[0] = b0.x; vb[1] = b0.y; vb[2] = b0.z; vb[3] = b0.w;
+                vb[4] = b1.x; vb[5] = b1.y; vb[6] = b1.z; vb[7] = b1.w;
+                const uint32_t off = kmajor_off(row, kg);
+                store_split_row(sAop, off, va);
+                store_split_row(sBop, off, vb);
+            }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        // this stage is consumed: start the copies of the pair-of-pairs two steps ahead
+        issue_raw(q + 2 * gridDim.x, stage);
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t a0 = smem_u32(sAop), b0 = smem_u32(sBop);
@@ -204,7 +232,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a)
                          : "memory");
         }
-        if (q + (int)gridDim.x < npp) load(q + gridDim.x);
         bool ok = mbar_wait(bar_a, phase);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) { atomicExch(&g_tc_error, 1); s_abort = 1; }
@@ -245,6 +272,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy may land after the block is gone
     __syncthreads();
     if (s_abort) mbar_wait(bar_a, phase);  // give an MMA still in flight a bounded chance to land
     __syncthreads();
@@ -257,8 +285,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 bool tc_gemm_eligible(int m, int n, int k, int64_t sA, int64_t sB, int64_t sC, const void *A, const void *B,
                       const void *C) {
     if (m != 64 || n != 64 || k != 64) return false;
+    // 16-byte copies of whole matrices: both operands 16-byte aligned, strides multiples of 4 floats
+    if (((uintptr_t)A & 15) != 0 || (sA % 4) != 0) return false;
     if (((uintptr_t)B & 15) != 0 || (sB % 4) != 0) return false;
-    (void)sA; (void)sC; (void)A; (void)C;
+    (void)sC; (void)C;
     return true;
 }
 
