@@ -61,30 +61,30 @@ __device__ __forceinline__ uint32_t kmajor_off(int row, int kgroup) {
     return (uint32_t)((row >> 3) * 1024 + kgroup * 128 + (row & 7) * 16);
 }
 
-__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
-    h = __float2bfloat16_rn(x);
-    float r1 = x - __bfloat162float(h);
-    m = __float2bfloat16_rn(r1);
-    float r2 = r1 - __bfloat162float(m);
-    l = __float2bfloat16_rn(r2);
+// Exact three-way BF16 split of two values at once: each cvt.rn.bf16x2
+// rounds and packs a pair (element 0 in the low half), and a BF16 value
+// widens back to FP32 by placing its bits in the high half of a word.
+__device__ __forceinline__ uint32_t bf16x2_rn(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
 }
-
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
-    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+__device__ __forceinline__ void split3x2(float x0, float x1, uint32_t &H, uint32_t &M, uint32_t &L) {
+    H = bf16x2_rn(x0, x1);
+    const float r0 = x0 - __uint_as_float(H << 16), r1 = x1 - __uint_as_float(H & 0xffff0000u);
+    M = bf16x2_rn(r0, r1);
+    const float s0 = r0 - __uint_as_float(M << 16), s1 = r1 - __uint_as_float(M & 0xffff0000u);
+    L = bf16x2_rn(s0, s1);
 }
 
 // Split 8 K-consecutive fp32 values of one operand row into three 16-byte
 // core-matrix rows.
 __device__ __forceinline__ void store_split_row(unsigned char *base, uint32_t off, const float (&v)[8]) {
-    __nv_bfloat16 h[8], m[8], l[8];
+    uint32_t h[4], m[4], l[4];
 #pragma unroll
-    for (int e = 0; e < 8; e++) split3(v[e], h[e], m[e], l[e]);
-    uint4 H = make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
-    uint4 M = make_uint4(pack2(m[0], m[1]), pack2(m[2], m[3]), pack2(m[4], m[5]), pack2(m[6], m[7]));
-    uint4 L = make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
-    *reinterpret_cast<uint4 *>(base + 0 * TC_TILE_BYTES + off) = H;
-    *reinterpret_cast<uint4 *>(base + 1 * TC_TILE_BYTES + off) = M;
-    *reinterpret_cast<uint4 *>(base + 2 * TC_TILE_BYTES + off) = L;
+    for (int e = 0; e < 4; e++) split3x2(v[2 * e], v[2 * e + 1], h[e], m[e], l[e]);
+    *reinterpret_cast<uint4 *>(base + 0 * TC_TILE_BYTES + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(base + 1 * TC_TILE_BYTES + off) = make_uint4(m[0], m[1], m[2], m[3]);
+    *reinterpret_cast<uint4 *>(base + 2 * TC_TILE_BYTES + off) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
