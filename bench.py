@@ -50,8 +50,9 @@ FFMA_TFLOPS = 77.96
 GEMM_BYTES_PER_PAIR = 3 * 64 * 64 * 4                       # A, B in; C out
 GEMM_FLOPS_PER_PAIR = 2 * 64 ** 3
 LS_M, LS_N, LS_RHS = 128, 32, 4
-# A and B in; A (overwritten with the QR factors) and B (x in rows < n, (Q^T b) below) out
-LS_BYTES_PER_MATRIX = 4 * 2 * (LS_M * LS_N + LS_M * LS_RHS)
+# per-system algorithmic bytes: A and B in, x out (the factors written back over A
+# and the rows of B below n are not counted)
+LS_BYTES_PER_MATRIX = 4 * (LS_M * LS_N + LS_M * LS_RHS + LS_N * LS_RHS)
 LS_FLOPS_PER_MATRIX = (2 * LS_M * LS_N ** 2 - 2 * LS_N ** 3 // 3
                        + LS_RHS * (4 * LS_M * LS_N - 2 * LS_N ** 2 + LS_N ** 2))
 
