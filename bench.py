@@ -482,12 +482,15 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
 
     pk = peaks()
     rl = {}
-    for name, t, bytes_, units_k in (("gemm", t_gemm, GEMM_BYTES_PER_PAIR, kg), ("gels", t_ls, LS_BYTES_PER_MATRIX, kl)):
+    for name, t, bytes_, flops_, units_k in (("gemm", t_gemm, GEMM_BYTES_PER_PAIR, GEMM_FLOPS_PER_PAIR, kg),
+                                             ("gels", t_ls, LS_BYTES_PER_MATRIX, LS_FLOPS_PER_MATRIX, kl)):
         ach = bytes_ * units_k / t / 1e9
         tr = traffic_for(name + "_d2")
         rl[name] = {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                     "frac": ach / pk["hbm_gbs"], "traffic": tr, "ms": t * 1e3,
-                    "algorithmic_bytes_per_launch": bytes_ * units_k, "peak_source": pk["source"] + " hbm_gbs"}
+                    "algorithmic_bytes_per_launch": bytes_ * units_k, "peak_source": pk["source"] + " hbm_gbs",
+                    # the same launch against the FP32 FFMA rate (algorithmic flops, LAPACK counts)
+                    "fp32_tflops": flops_ * units_k / t / 1e12, "fp32_frac": flops_ * units_k / t / 1e12 / FFMA_TFLOPS}
     dom = "gemm" if t_gemm >= t_ls else "gels"
     value = units_all / elapsed_max
     line = {
