@@ -289,7 +289,7 @@ __device__ __forceinline__ float refine_ls(const QF &q, const float *A0, int lda
 // SOLVE = false: factorisation only (the solve of gbla_sgels_batched_ws runs
 // in k_ls_solve); F (nullable) receives the factors instead of A.
 template <typename T, int R, bool SOLVE = true>
-__global__ void __launch_bounds__(128, SOLVE ? 1 : 3)
+__global__ void __launch_bounds__(128, (SOLVE || sizeof(T) == 8) ? 1 : 3)
     k_qr_warp(int m, int n, int nrhs, T *__restrict__ A, int64_t sA, T *__restrict__ B, int64_t sB,
               T *__restrict__ tau_g, int64_t sTau, int *__restrict__ info, int flags, int refine, int batch,
               T *__restrict__ F = nullptr, int64_t sF = 0) {
@@ -730,6 +730,16 @@ static gbla_status qr_launch(int m, int n, int nrhs, T *A, int64_t sA, T *B, int
                                       (T *)nullptr, (int64_t)0);
         return launch_status();
     };
+    if (!(flags & QR_SOLVE) || nrhs == 0) {
+        // factorisation only (geqrf): the variant without the solve code needs
+        // fewer registers and fits three blocks per SM
+        switch (R) {
+            case 1: return go(k_qr_warp<T, 1, false>);
+            case 2: return go(k_qr_warp<T, 2, false>);
+            case 3: return go(k_qr_warp<T, 3, false>);
+            default: return go(k_qr_warp<T, 4, false>);
+        }
+    }
     switch (R) {
         case 1: return go(k_qr_warp<T, 1>);
         case 2: return go(k_qr_warp<T, 2>);
