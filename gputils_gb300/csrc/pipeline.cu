@@ -96,6 +96,12 @@ int64_t default_chunk(int64_t batch, int64_t min_chunk) {
 
 char *align256(void *p) { return reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255)); }
 
+// The pipeline's streams and buffers belong to the device it was created on.
+bool on_own_device(const gbla_stream_pipeline *p) {
+    int dev = -1;
+    return cudaGetDevice(&dev) == cudaSuccess && dev == p->device;
+}
+
 }  // namespace
 
 }  // namespace gbla
@@ -140,6 +146,7 @@ GBLA_API gbla_status gbla_sgemm_batched_host(gbla_stream_pipeline *p, int m, int
                                              cudaStream_t st) {
     if (!p || m < 0 || n < 0 || k < 0 || batch < 0 || chunk < 0) return GBLA_INVALID_VALUE;
     if (batch == 0 || m == 0 || n == 0) return GBLA_SUCCESS;
+    if (!on_own_device(p)) return GBLA_INVALID_VALUE;
     const int64_t ea = (int64_t)m * k, eb = (int64_t)k * n, ec = (int64_t)m * n;
     if ((ea > 0 && (!A || sA < ea)) || (eb > 0 && (!B || sB < eb)) || !Cm || sC < ec) return GBLA_INVALID_VALUE;
     const int64_t cs = chunk > 0 ? (chunk < batch ? chunk : batch) : default_chunk(batch, 1024);
@@ -172,6 +179,7 @@ GBLA_API gbla_status gbla_sgels_batched_host(gbla_stream_pipeline *p, int m, int
                                              int refine, int batch, int chunk, cudaStream_t st) {
     if (!p || m < 0 || n < 0 || nrhs < 0 || batch < 0 || chunk < 0 || refine < 0 || m < n) return GBLA_INVALID_VALUE;
     if (batch == 0 || n == 0) return GBLA_SUCCESS;
+    if (!on_own_device(p)) return GBLA_INVALID_VALUE;
     const int64_t ea = (int64_t)m * n, eb = (int64_t)m * nrhs;
     if (!A || sA < ea || (nrhs > 0 && (!B || !X || sB < eb))) return GBLA_INVALID_VALUE;
     if (m > 128 || n > 32) return GBLA_NOT_SUPPORTED;

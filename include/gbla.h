@@ -222,7 +222,8 @@ gbla_status gbla_sgels_batched_ws(int m, int n, int nrhs, float *A, int64_t stri
  * workers, so that copies in, kernels and copies out of consecutive chunks
  * overlap.  The calls are ordered on `stream` like a kernel launch: host
  * buffers must stay valid, and results are available, once `stream` has
- * reached that point.  One pipeline serves one stream at a time.  Replaces
+ * reached that point.  One pipeline serves one stream at a time, on the
+ * device that was current when it was created (other devices: invalid value).  Replaces
  * the synchronous upload -> call -> download sequence of DTensor
  * (include/tensor.cuh:875-884, 1129-1154) around addAB and
  * leastSquaresBatched. */
