@@ -358,17 +358,22 @@ __global__ void __launch_bounds__(128, (SOLVE || sizeof(T) == 8) ? 1 : 3)
 }
 
 // ------------------------------------------ solve from stored factors
-// The QrWarp interface over factors held in shared memory (column-major,
-// 32 R padded rows): the same values and the same operation order as the
-// register-resident version, so both give bit-identical solutions.
+// The QrWarp interface over factors held in shared memory, column-major with
+// column stride LDQ = 32 R + 1: a column (lanes on consecutive rows) and a
+// row of R (lane l reading R(j, l)) are both free of bank conflicts.  The
+// reflector applications and the back substitution follow QrWarp operation
+// for operation; the substitution with R^T runs column by column (a row of R
+// per step) instead of with one warp reduction per step.
 template <int R>
 struct QrSmem {
-    const float *Q;  // Q[j * 32 R + i] = factor element (i, j)
+    static constexpr int LDQ = 32 * R + 1;
+    const float *Q;  // Q[j * LDQ + i] = factor element (i, j)
     float dinv;
     int lane;
 
     __device__ __forceinline__ int row(int t) const { return lane + 32 * t; }
-    __device__ __forceinline__ float at(int t, int k) const { return Q[k * 32 * R + row(t)]; }
+    __device__ __forceinline__ float at(int t, int k) const { return Q[k * LDQ + row(t)]; }
+    __device__ __forceinline__ float rt(int j) const { return Q[lane * LDQ + j]; }  // R(j, lane)
 
     // Reflector k < 32: rows 32 t (t >= 1) are all below the diagonal.
     __device__ __forceinline__ float vk(int t, int k) const {
@@ -401,13 +406,15 @@ struct QrSmem {
         }
         return z;
     }
+    // Solve R^T h = g (g in lane j); returns h in lane j.  After h_j is known
+    // every later row l subtracts R(j, l) h_j from its g_l.
     __device__ __forceinline__ float forward_solve_rt(int n, float g) const {
         float h = 0.f;
+        const bool live = lane < n;
         for (int j = 0; j < n; j++) {
-            float part = lane < j ? at(0, j) * h : 0.f;
-            float sm = warp_sum(part);
-            float hj = shfl((g - sm) * dinv, j);
+            const float hj = shfl(g * dinv, j);
             if (lane == j) h = hj;
+            if (live && lane > j) g = fmaf(-rt(j), hj, g);
         }
         return h;
     }
@@ -432,12 +439,12 @@ template <int R>
 __device__ __forceinline__ void ls_solve_block(int m, int n, int nrhs, const float *Q, const float *A0,
                                                const float *taus, float *a_g, float *b_g, int refine, int warp,
                                                int lane) {
-    constexpr int LDM = 32 * R;
+    constexpr int LDM = 32 * R, LDQ = QrSmem<R>::LDQ;
     QrSmem<R> q;
     q.Q = Q;
     q.lane = lane;
     {
-        const float d = lane < n ? Q[lane * LDM + lane] : 0.f;
+        const float d = lane < n ? Q[lane * LDQ + lane] : 0.f;
         q.dinv = (lane < n && d != 0.f) ? 1.f / d : 0.f;
     }
     for (int c = warp; c < nrhs; c += 4) {
@@ -462,7 +469,7 @@ __device__ __forceinline__ void ls_solve_block(int m, int n, int nrhs, const flo
 #pragma unroll
         for (int t = 0; t < R; t++) {
             const int i = lane + 32 * t;
-            if (i < m) a_g[(int64_t)j * m + i] = Q[j * LDM + i];
+            if (i < m) a_g[(int64_t)j * m + i] = Q[j * LDQ + i];
         }
     }
 }
@@ -475,9 +482,9 @@ __global__ void __launch_bounds__(128)
     k_ls_solve(int m, int n, int nrhs, float *__restrict__ A, int64_t sA, const float *__restrict__ F,
                const float *__restrict__ tau_g, float *__restrict__ B, int64_t sB, int refine, int batch) {
     extern __shared__ __align__(16) float lsm[];
-    constexpr int LDM = 32 * R;
-    float *Q = lsm;                // n columns x LDM: factors
-    float *A0 = Q + 32 * LDM;      // n columns x LDM: original matrix (refinement only)
+    constexpr int LDM = 32 * R, LDQ = QrSmem<R>::LDQ;
+    float *Q = lsm;                // n columns x LDQ: factors
+    float *A0 = Q + 32 * LDQ;      // n columns x LDM: original matrix (refinement only)
     float *taus = A0 + (refine > 0 ? 32 * LDM : 0);  // 32
     const int64_t mat = blockIdx.x;
     if (mat >= batch) return;
@@ -489,7 +496,7 @@ __global__ void __launch_bounds__(128)
         for (int t = 0; t < R; t++) {
             const int i = lane + 32 * t;
             const bool ok = i < m;
-            cp_async4(Q + j * LDM + i, f + (ok ? (int64_t)j * m + i : 0), ok);
+            cp_async4(Q + j * LDQ + i, f + (ok ? (int64_t)j * m + i : 0), ok);
             if (refine > 0) cp_async4(A0 + j * LDM + i, a_g + (ok ? (int64_t)j * m + i : 0), ok);
         }
     }
@@ -541,9 +548,9 @@ __global__ void __launch_bounds__(128)
     k_gels_cta(int m, int n, int nrhs, float *__restrict__ A, int64_t sA, float *__restrict__ B, int64_t sB,
                int *__restrict__ info, int refine, int batch) {
     extern __shared__ __align__(16) float gsm[];
-    constexpr int LDM = 32 * R;
-    float *Q = gsm;                           // 32 columns x LDM: factors
-    float *vbuf = Q + 32 * LDM;               // 2 x LDM: Householder vector of the step (double-buffered)
+    constexpr int LDM = 32 * R, LDQ = QrSmem<R>::LDQ;
+    float *Q = gsm;                           // 32 columns x LDQ: factors
+    float *vbuf = Q + 32 * LDQ;               // 2 x LDM: Householder vector of the step (double-buffered)
     float *taus = vbuf + 2 * LDM;             // 32
     float *A0 = taus + 32;                    // 32 columns x LDM: original matrix (refinement only)
     const int64_t mat = blockIdx.x;
@@ -631,11 +638,11 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
     for (int c = 0; c < 8; c++)
 #pragma unroll
-        for (int t = 0; t < R; t++) Q[(warp + 4 * c) * LDM + lane + 32 * t] = a[t][c];
+        for (int t = 0; t < R; t++) Q[(warp + 4 * c) * LDQ + lane + 32 * t] = a[t][c];
     __syncthreads();
     if (warp == 0) {
         // info: first k whose diagonal entry R_kk is exactly zero (1-based)
-        const unsigned zero = __ballot_sync(FULL, lane < n && Q[lane * LDM + lane] == 0.f);
+        const unsigned zero = __ballot_sync(FULL, lane < n && Q[lane * LDQ + lane] == 0.f);
         if (info && lane == 0) info[mat] = zero ? __ffs(zero) : 0;
     }
     ls_solve_block<R>(m, n, nrhs, Q, A0, taus, a_g, B + mat * sB, refine, warp, lane);
@@ -757,7 +764,7 @@ static gbla_status gels_cta_launch(int m, int n, int nrhs, float *A, int64_t sA,
     if (m > 128 || n > 32) return GBLA_NOT_SUPPORTED;
     const int R = (m + 31) / 32;
     // factors, two Householder vectors, taus, and the original A when refining
-    const size_t smem = sizeof(float) * ((size_t)(refine > 0 ? 2 : 1) * 32 * 32 * R + 2 * 32 * R + 32);
+    const size_t smem = sizeof(float) * ((size_t)32 * (32 * R + 1) + (refine > 0 ? 32 * 32 * R : 0) + 2 * 32 * R + 32);
     auto go = [&](auto kern) -> gbla_status {
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -792,7 +799,7 @@ static gbla_status gels_ws_launch(int m, int n, int nrhs, float *A, int64_t sA, 
     const int R = (m + 31) / 32;
     const unsigned g1 = (unsigned)((batch + 3) / 4);
     const size_t smem1 = (size_t)4 * 32 * sizeof(float);
-    const size_t smem2 = sizeof(float) * ((size_t)(refine > 0 ? 2 : 1) * 32 * 32 * R + 32);
+    const size_t smem2 = sizeof(float) * ((size_t)32 * (32 * R + 1) + (refine > 0 ? 32 * 32 * R : 0) + 32);
     auto go = [&](auto kf, auto ks) -> gbla_status {
         kf<<<g1, 128, smem1, st>>>(m, n, 0, A, sA, nullptr, 0, tau, 32, info, QR_WRITE_FACTORS | QR_WRITE_TAU, 0,
                                    batch, F, (int64_t)m * n);
