@@ -1,6 +1,6 @@
 // diag.cu -- arithmetic-throughput probe used for the roofline denominators
-// of the CUDA-core-bound kernels (FP32 FFMA and FP64 DFMA peaks are not part
-// of the measured peaks).
+// of the CUDA-core-bound kernels (the measured peak figures cover HBM
+// bandwidth and BF16 tensor throughput only, not FP32 FFMA or FP64 DFMA).
 #include "common.cuh"
 
 namespace gbla {
