@@ -37,7 +37,7 @@ typedef struct CUstream_st *cudaStream_t;
 typedef enum gbla_status {
     GBLA_SUCCESS = 0,
     GBLA_INVALID_VALUE = 1,    /* a size, stride or pointer argument is invalid */
-    GBLA_NOT_SUPPORTED = 2,    /* valid request outside what this build implements */
+    GBLA_NOT_SUPPORTED = 2,    /* valid request outside what this library implements */
     GBLA_CUDA_ERROR = 3,       /* a CUDA runtime call or kernel launch failed */
     GBLA_WORKSPACE_TOO_SMALL = 4
 } gbla_status;

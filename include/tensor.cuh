@@ -110,7 +110,7 @@ inline void gpuAssert(gbla_status code, const char *file, int line, bool abort =
 }
 
 namespace gputils_detail {
-// A library call that rejects a size this build does not implement becomes
+// A library call that rejects a size the library does not implement becomes
 // std::invalid_argument (the reference's exception for unusable shapes);
 // every other failure is a library error: print and exit, as gpuErrChk does.
 inline void check(gbla_status s, const char *what) {

@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (libgbla.so, the include/ headers,
  * the drop-in tensor.cuh) links, loads or calls this file.  Only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, and only as
- * the checker / the timed host baseline.
+ * the reference values of the parity tests / the timed host baseline.
  *
  * The reference (GPUEngineering/GPUtils, include/tensor.cuh) has no CPU code:
  * every numeric call on the path goes to cuBLAS 13.1 / cuSOLVER 12.0 (CUDA

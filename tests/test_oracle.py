@@ -1,4 +1,4 @@
-"""Pins the FP64 oracle (oracle/oracle.c) before it is trusted as a checker:
+"""Pins the FP64 oracle (oracle/oracle.c) before the parity tests rely on it:
 against every golden value the reference's own tests hold for the hot path
 (read from test/testTensor.cu into tests/golden/reference_goldens.json) and
 against numpy/scipy LAPACK on random inputs.  CPU only."""
