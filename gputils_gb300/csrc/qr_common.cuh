@@ -5,7 +5,8 @@
 // (the fused FP32 least-squares kernel).  Each kernel instantiation is used
 // by one translation unit only.
 //
-// Layout: one warp per matrix (m <= 128, n <= 32).  Lane l owns rows
+// Warp kernels (k_qr_warp, k_ormqr_warp): one warp per matrix (m <= 128,
+// n <= 32).  Lane l owns rows
 // l + 32 t (t < R = ceil(m/32)) of A in registers; the Householder vector of
 // step k lives in column k below the diagonal (LAPACK dgeqr2/dlarfg
 // convention: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta).  The
@@ -437,8 +438,8 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 // Solve phase shared by k_ls_solve and k_gels_cta: factors (Q, column-major,
-// 32 R rows), taus and the original A (A0, refinement only) are in shared
-// memory; one warp per right-hand side solves in FP32 and refines with
+// column stride 32 R + 1), taus and the original A (A0, refinement only,
+// column stride 32 R, zero-padded rows) are in shared memory; one warp per right-hand side solves in FP32 and refines with
 // double-FP32 residuals, then the block copies the factors into A.
 template <int R>
 __device__ __forceinline__ void ls_solve_block(int m, int n, int nrhs, const float *Q, const float *A0,
@@ -543,11 +544,11 @@ __device__ __forceinline__ float reduce_scatter8(const float (&p)[8], int lane) 
 // (warp k mod 4) forms the Householder vector exactly as QrWarp::factor does
 // and publishes it (explicit unit diagonal, double-buffered) in shared
 // memory; after one block barrier every warp applies the reflector to its
-// columns j > k.  The
-// per-lane partial dot products and the reduction tree are those of
-// QrWarp::factor, so factors, solutions and info are bit-identical to the
-// one-warp-per-system kernel.  Then the factors go to shared memory and
-// ls_solve_block solves one right-hand side per warp.
+// columns j > k.  The per-lane partial dot products and the reduction tree
+// are those of QrWarp::factor, so factors and info are bit-identical to
+// k_qr_warp's, and the solutions to the two-kernel schedule's (both solve
+// through QrSmem).  Then the factors go to shared memory and ls_solve_block
+// solves one right-hand side per warp.
 template <int R>
 __global__ void __launch_bounds__(128)
     k_gels_cta(int m, int n, int nrhs, float *__restrict__ A, int64_t sA, float *__restrict__ B, int64_t sB,
