@@ -44,8 +44,10 @@ import numpy as np  # noqa: E402
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic.json")
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
-# FP32 FFMA rate measured on this GB300 with gbla_diag_fma_throughput (profiles/peaks_fma.md)
-FFMA_TFLOPS = 77.96
+# FP32 FFMA rate of this GPU, measured by the FMA probe (baseline/peak_probe.cu) at
+# start-up while the SM clock is sampled (fp32_peak()); the denominator of the
+# CUDA-core rooflines
+FP32_PEAK = {"tflops": None, "sm_mhz": None, "source": None}
 
 # algorithmic work per unit (each input read once, each output written once)
 GEMM_BYTES_PER_PAIR = 3 * 64 * 64 * 4                       # A, B in; C out
@@ -73,6 +75,10 @@ def parse_args(argv=None):
     ap.add_argument("--no-reference-library", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
     ap.add_argument("--peaks", action="store_true", help="print the measured FFMA / DFMA rates and exit")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="fraction of the workload's batch to run (small cases for ncu captures)")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="d2: skip the other configurations' results in the default line")
     ap.add_argument("--no-autotune", action="store_true", help="d3: keep the plan's default launch configuration")
     ap.add_argument("--ws-pairs", type=int, default=200_000, help="d5: (A, V) training pairs of the warm-start net")
     ap.add_argument("--ws-epochs", type=int, default=20, help="d5: training epochs of the warm-start net")
@@ -199,6 +205,17 @@ def rel_err(x, ref):
     return float((num / np.where(den == 0, 1, den)).max())
 
 
+def rel_err_t(x, ref, k):
+    """max over k matrices of ||x_i - ref_i|| / ||ref_i|| (FP64, on the device);
+    x and ref hold k equally sized matrices back to back."""
+    xd = x.reshape(k, -1).double()
+    rd = ref.reshape(k, -1).double()
+    num = (xd - rd).norm(dim=1)
+    den = rd.norm(dim=1)
+    den = den.where(den > 0, den.new_ones(()))
+    return float((num / den).max())
+
+
 # ------------------------------------------------------------ CPU baseline
 def _repeat_timed(fn, seconds: float):
     """Run fn() until `seconds` have passed (at least once); returns (calls, total seconds)."""
@@ -320,33 +337,46 @@ def metric_name(workload):
     return "matrices/s on 1 GB300 (Chol/QR/SVD batched) vs ref cuSOLVER build at equal FP64 err"
 
 
+def _k(count, args):
+    """Batch count of a workload at the --scale fraction (at least 1)."""
+    scale = getattr(args, "scale", 1.0) if args is not None else 1.0
+    return max(1, int(round(count * scale)))
+
+
 def workload_config(workload, args=None):
+    """The configuration dict of a workload; both arms print the same one."""
+    refine = getattr(args, "refine", 1) if args is not None else 1
+    scale = getattr(args, "scale", 1.0) if args is not None else 1.0
+    extra = {} if scale == 1.0 else {"scale": scale}
     if workload == "d2":
-        return {"workload": "precision: addAB 16384 x 64x64x64 fp32 (BF16x6 tcgen05) + leastSquaresBatched "
-                            "8192 x 128x32 fp32, 4 RHS, kappa 1e3 (FP32 QR + double-FP32 refinement)",
-                "gemm_pairs": 16384, "ls_systems": 8192, "parallelism": "replicas",
-                "l2": "inputs larger than L2 every step (per-step copies of the least-squares inputs)"}
+        return dict({"workload": "precision: addAB 16384 x 64x64x64 fp32 (BF16x6 tcgen05) + leastSquaresBatched "
+                                 "8192 x 128x32 fp32, 4 RHS, kappa 1e3 (FP32 QR + double-FP32 refinement)",
+                     "gemm_pairs": _k(16384, args), "ls_systems": _k(8192, args), "refine_steps": refine,
+                     "parallelism": "replicas",
+                     "l2": "inputs larger than L2 every step (per-step copies of the least-squares inputs)"}, **extra)
     if workload == "d1":
-        return {"workload": "Cholesky factor+solve 4096 x 16x16 fp32, 1 RHS (CholeskyBatchFactoriser API: potrf + potrs)",
-                "matrices": 4096, "parallelism": "replicas",
-                "l2": "L2 flushed between timed steps (the 4.5 MB working set fits in L2)"}
+        return dict({"workload": "Cholesky factor+solve 4096 x 16x16 fp32, 1 RHS (CholeskyBatchFactoriser API: "
+                                 "potrf + potrs)",
+                     "matrices": _k(4096, args), "parallelism": "replicas",
+                     "l2": "L2 flushed between timed steps (the 4.5 MB working set fits in L2)"}, **extra)
     if workload == "d3":
         dt = getattr(args, "dtype", "f32") if args is not None else "f32"
-        return {"workload": f"ragged Cholesky factor+solve, 20000 SPD systems, n log-uniform in [4,128], "
-                            f"nrhs 1..8, {dt}, one call (plan + CUDA graph), FP32 factor + refinement",
-                "systems": 20000, "dtype": dt, "parallelism": "replicas",
-                "l2": "inputs larger than L2 every step (per-step copies of the arenas)"}
+        return dict({"workload": f"ragged Cholesky factor+solve, 20000 SPD systems, n log-uniform in [4,128], "
+                                 f"nrhs 1..8, {dt}, one call (plan + CUDA graph), FP32 factor + refinement",
+                     "systems": _k(20000, args), "dtype": dt, "refine_steps": 1 if dt == "f32" else 2,
+                     "parallelism": "replicas",
+                     "l2": "inputs larger than L2 every step (per-step copies of the arenas)"}, **extra)
     if workload == "d5":
         pairs = getattr(args, "ws_pairs", 200_000) if args is not None else 200_000
-        return {"workload": "learned warm start: one-sided Jacobi SVD (S and V^T) of 32768 64x64 fp32 matrices of "
-                            "the parametric family A0 + sum theta_j A_j, tol 1e-6; each step = network "
-                            "(4096->512->512->2016, BF16 tcgen05) + Cayley frame + warm Jacobi with cold fallback",
-                "matrices": 32768, "n": 64, "train_pairs": pairs, "parallelism": "replicas",
-                "l2": "inputs (537 MB) larger than L2"}
-    return {"workload": "one-sided Jacobi SVD (Svd::factorise, S and V^T) of 8192 32x32 fp32 matrices of the "
-                        "parametric family A0 + sum theta_j A_j, tol 1e-6, cold start",
-            "matrices": 8192, "n": 32, "parallelism": "replicas",
-            "l2": "per-step copies of the input (the SVD destroys it)"}
+        return dict({"workload": "learned warm start: one-sided Jacobi SVD (S and V^T) of 32768 64x64 fp32 matrices "
+                                 "of the parametric family A0 + sum theta_j A_j, tol 1e-6; each step = network "
+                                 "(4096->512->512->2016, BF16 tcgen05) + Cayley frame + warm Jacobi with cold fallback",
+                     "matrices": _k(32768, args), "n": 64, "train_pairs": pairs, "parallelism": "replicas",
+                     "l2": "inputs (537 MB) larger than L2"}, **extra)
+    return dict({"workload": "one-sided Jacobi SVD (Svd::factorise, S and V^T) of 8192 32x32 fp32 matrices of the "
+                             "parametric family A0 + sum theta_j A_j, tol 1e-6, cold start",
+                 "matrices": _k(8192, args), "n": 32, "parallelism": "replicas",
+                 "l2": "per-step copies of the input (the SVD destroys it)"}, **extra)
 
 
 # ------------------------------------------------------------- ours: d2
@@ -383,8 +413,8 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
     from gputils_gb300 import workloads, _lib
     from oracle import oracle as O
 
-    A, B = workloads.d2a_gemm()
-    LA, LB = workloads.d2b_least_squares()
+    A, B = workloads.d2a_gemm(k=_k(16384, args))
+    LA, LB = workloads.d2b_least_squares(k=_k(8192, args))
     kg, kl = A.shape[0], LA.shape[0]
     Ag, Bg = to_dev(A, dev), to_dev(B, dev)
     Cg = torch.empty_like(Ag)
@@ -476,7 +506,7 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
     reflib = None
     if not args.no_reference_library:
         try:
-            reflib = reference_library_d2(dev, st, Ag, Bg, Cg, LA0, LB0, A, B, LA, LB)
+            reflib = reference_library_d2(dev, st, Ag, Bg, Cg, LA0, LB0, A, B, LA, LB, LBs[args.warmup])
         except Exception as exc:  # reported, never fatal for our own numbers
             reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
 
@@ -490,7 +520,8 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
                     "frac": ach / pk["hbm_gbs"], "traffic": tr, "ms": t * 1e3,
                     "algorithmic_bytes_per_launch": bytes_ * units_k, "peak_source": pk["source"] + " hbm_gbs",
                     # the same launch against the FP32 FFMA rate (algorithmic flops, LAPACK counts)
-                    "fp32_tflops": flops_ * units_k / t / 1e12, "fp32_frac": flops_ * units_k / t / 1e12 / FFMA_TFLOPS}
+                    "fp32_tflops": flops_ * units_k / t / 1e12,
+                    "fp32_frac": flops_ * units_k / t / 1e12 / FP32_PEAK["tflops"]}
     dom = "gemm" if t_gemm >= t_ls else "gels"
     value = units_all / elapsed_max
     line = {
@@ -498,7 +529,7 @@ def run_ours_d2(args, dev, st, L, rank, world, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_max / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded numpy generators, configuration distributions)",
-        "config": dict(workload_config("d2", args), refine_steps=args.refine),
+        "config": workload_config("d2", args),
         "roofline": dict(rl[dom], kernel=dom),
         "roofline_all": rl,
         "max_rel_err_vs_fp64": {"gemm": err_gemm, "least_squares_x": err_ls},
@@ -519,7 +550,7 @@ def gbla_device_flags_ok(L):
     return L.gbla_device_error_flags() == 0
 
 
-def reference_library_d2(dev, st, Ag, Bg, Cg, LA0, LB0, A, B, LA, LB):
+def reference_library_d2(dev, st, Ag, Bg, Cg, LA0, LB0, A, B, LA, LB, X_ours):
     """The reference's calls on the same inputs: cublasSgemmBatched with
     pointer arrays (addAB) and cublasSgelsBatched (nrhs = 1, so the 4 RHS run
     as one call on a 4x-replicated batch; replication not timed)."""
@@ -563,8 +594,13 @@ def reference_library_d2(dev, st, Ag, Bg, Cg, LA0, LB0, A, B, LA, LB):
     idl = np.arange(0, kl, 64)
     _, Xo = O.gels(LA[idl], LB[idl])
     err_l = rel_err(X[idl], Xo[:, :n])
+    # ours against the reference library's own output, every matrix
+    Xr = LBr.reshape(kl, r, m)[:, :, :n]
+    Xu = X_ours.reshape(kl, r, m)[:, :, :n]
+    vs_ref = {"gemm": rel_err_t(Cg, Cr, kg), "least_squares_x": rel_err_t(Xu, Xr, kl)}
     return {"value": (kg + kl) / (tg + tl), "unit": "matrices/s", "gemm_ms": tg * 1e3, "gels_ms": tl * 1e3,
             "max_rel_err_vs_fp64": {"gemm": err_g, "least_squares_x": err_l},
+            "ours_max_rel_err_vs_reference_output": vs_ref,
             "calls": "cublasSgemmBatched (pointer arrays) + cublasSgelsBatched on the 4x-replicated batch "
                      "(one call; nrhs = 1 in the reference API)"}
 
@@ -592,7 +628,7 @@ def run_ours_d3(args, dev, st, L, rank, world, dist):
 
     dt = np.float32 if args.dtype == "f32" else np.float64
     tdt = torch.float32 if dt == np.float32 else torch.float64
-    n, nrhs, a_off, b_off, A, B = workloads.d3_ragged(dtype=dt)
+    n, nrhs, a_off, b_off, A, B = workloads.d3_ragged(count=_k(20000, args), dtype=dt)
     count = len(n)
     plan = C.c_void_p()
     _lib.check(L.gbla_ragged_plan_create(np.ascontiguousarray(a_off).ctypes.data,
@@ -688,7 +724,7 @@ def run_ours_d3(args, dev, st, L, rank, world, dist):
     reflib = None
     if not args.no_reference_library:
         try:
-            reflib = reference_library_d3(dev, st, n, nrhs, a_off, b_off, A0, B0, dt)
+            reflib = reference_library_d3(dev, st, n, nrhs, a_off, b_off, A0, B0, dt, Bs[args.warmup])
         except Exception as exc:
             reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
     _lib.check(L.gbla_ragged_plan_destroy(plan), "plan destroy")
@@ -703,7 +739,7 @@ def run_ours_d3(args, dev, st, L, rank, world, dist):
         "metric": metric_name("d3"), "value": units_all / elapsed_max, "unit": "matrices/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded)",
-        "config": dict(workload_config("d3", args), refine_steps=refine, launch_config=tuning),
+        "config": workload_config("d3", args), "launch_config": tuning,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": ach / pk["hbm_gbs"], "traffic": traffic_for("ragged_d3_" + args.dtype),
                      "kernel": "posv_ragged (all kernels of one call)", "algorithmic_bytes_per_launch": bytes_},
@@ -715,7 +751,7 @@ def run_ours_d3(args, dev, st, L, rank, world, dist):
     }
 
 
-def reference_library_d3(dev, st, n, nrhs, a_off, b_off, A0, B0, dt):
+def reference_library_d3(dev, st, n, nrhs, a_off, b_off, A0, B0, dt, X_ours):
     """The reference's way to solve a ragged batch: for each distinct n one
     potrfBatched over that size group (CholeskyBatchFactoriser::factorise),
     then one potrsBatched per right-hand-side column (solve takes nrhs = 1),
@@ -760,6 +796,7 @@ def reference_library_d3(dev, st, n, nrhs, a_off, b_off, A0, B0, dt):
         tot += e[0].elapsed_time(e[1]) / 1e3
     t = tot / reps
     X = B0.cpu().numpy()
+    Xu = X_ours.cpu().numpy()
     A0.copy_(Ac); B0.copy_(Bc)
     idx = np.arange(0, len(n), 41)
     err = 0.0
@@ -771,8 +808,17 @@ def reference_library_d3(dev, st, n, nrhs, a_off, b_off, A0, B0, dt):
         xo = np.linalg.solve(M, b)
         x = X[b_off[i]:b_off[i] + k * r].reshape(r, k).T
         err = max(err, float(np.linalg.norm(x - xo) / np.linalg.norm(xo)))
+    # ours against the reference library's output, every system
+    b_sz = n.astype(np.int64) * nrhs
+    ends = b_off + b_sz
+    vs_ref = 0.0
+    for i in range(len(n)):
+        xr = X[b_off[i]:ends[i]].astype(np.float64)
+        xu = Xu[b_off[i]:ends[i]].astype(np.float64)
+        d = np.linalg.norm(xr)
+        vs_ref = max(vs_ref, float(np.linalg.norm(xu - xr) / (d if d > 0 else 1.0)))
     return {"value": len(n) / t, "unit": "matrices/s", "ms": t * 1e3, "library_calls": len(calls),
-            "max_rel_err_vs_fp64": {"x": err},
+            "max_rel_err_vs_fp64": {"x": err}, "ours_max_rel_err_vs_reference_output": {"x": vs_ref},
             "calls": "per size n: cusolverDn<t>potrfBatched, then per RHS column cusolverDn<t>potrsBatched "
                      "(nrhs = 1) over the systems having that column"}
 
@@ -784,7 +830,7 @@ def run_ours_svd(args, dev, st, L, rank, world, dist):
     from oracle import oracle as O
 
     nmat = 32 if args.workload == "d4" else 64
-    Ah = workloads.d4_svd32() if args.workload == "d4" else workloads.d5_svd64()
+    Ah = workloads.d4_svd32(k=_k(8192, args)) if args.workload == "d4" else workloads.d5_svd64(k=_k(32768, args))
     k = Ah.shape[0]
     A0 = to_dev(Ah, dev)
     nsteps = args.warmup + args.steps
@@ -826,7 +872,8 @@ def run_ours_svd(args, dev, st, L, rank, world, dist):
     reflib = None
     if not args.no_reference_library:
         try:
-            reflib = reference_library_svd(dev, st, A0, Ah, nmat, args.ref_sample or (512 if nmat == 32 else 128))
+            reflib = reference_library_svd(dev, st, A0, Ah, nmat, args.ref_sample or (512 if nmat == 32 else 128),
+                                           S.reshape(k, nmat))
         except Exception as exc:
             reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
     pk = peaks()
@@ -837,10 +884,10 @@ def run_ours_svd(args, dev, st, L, rank, world, dist):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded parametric family)", "config": workload_config(args.workload, args),
-        "roofline": {"bound": "fp32 cuda cores", "achieved": flops / t / 1e12, "peak": FFMA_TFLOPS,
-                     "unit": "TFLOP/s", "frac": flops / t / 1e12 / FFMA_TFLOPS, "traffic": traffic_for("svd_d4"),
-                     "kernel": "gesvj", "algorithmic_flops_per_launch": flops,
-                     "peak_source": "measured FFMA rate (gbla_diag_fma_throughput)"},
+        "roofline": {"bound": "fp32 cuda cores", "achieved": flops / t / 1e12, "peak": FP32_PEAK["tflops"],
+                     "unit": "TFLOP/s", "frac": flops / t / 1e12 / FP32_PEAK["tflops"],
+                     "traffic": traffic_for("svd_d4"), "kernel": "gesvj", "algorithmic_flops_per_launch": flops,
+                     "peak_source": FP32_PEAK["source"]},
         "max_rel_err_vs_fp64": {"sigma": err}, "sweeps": {"mean": float(sw.mean()), "max": int(sw.max())},
         "gpu_launches": args.steps, "clocks": clk.summary(), "reference_library": reflib, "e2e": e2e,
     }
@@ -861,7 +908,7 @@ def run_ours_d5(args, dev, st, L, rank, world, dist):
                                       theta_seed=1234 + rank, seed=rank)
     torch.cuda.synchronize()
     train_s = time.time() - t0
-    Ah = workloads.d5_svd64()
+    Ah = workloads.d5_svd64(k=_k(32768, args))
     k = Ah.shape[0]
     A = torch.from_numpy(np.ascontiguousarray(Ah.transpose(0, 2, 1))).to(dev)
     V0 = torch.empty_like(A)
@@ -954,7 +1001,7 @@ def run_ours_d5(args, dev, st, L, rank, world, dist):
     reflib = None
     if not args.no_reference_library:
         try:
-            reflib = reference_library_svd(dev, st, A, Ah, n, args.ref_sample or 128)
+            reflib = reference_library_svd(dev, st, A, Ah, n, args.ref_sample or 128, S)
         except Exception as exc:
             reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
     t = elapsed_max / args.steps
@@ -968,11 +1015,11 @@ def run_ours_d5(args, dev, st, L, rank, world, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network: bf16)",
         "data": "synthetic (seeded parametric family; training pairs from a separate theta stream)",
         "config": workload_config(args.workload, args),
-        "roofline": {"bound": "fp32 cuda cores", "achieved": flops / t_jac / 1e12, "peak": FFMA_TFLOPS,
-                     "unit": "TFLOP/s", "frac": flops / t_jac / 1e12 / FFMA_TFLOPS,
+        "roofline": {"bound": "fp32 cuda cores", "achieved": flops / t_jac / 1e12, "peak": FP32_PEAK["tflops"],
+                     "unit": "TFLOP/s", "frac": flops / t_jac / 1e12 / FP32_PEAK["tflops"],
                      "traffic": traffic_for("svd_d5_warm"), "kernel": "gesvj (warm), its own launch time",
                      "algorithmic_flops_per_launch": flops,
-                     "peak_source": "measured FFMA rate (gbla_diag_fma_throughput)"},
+                     "peak_source": FP32_PEAK["source"]},
         "roofline_network": {"bound": "tensor", "achieved": mlp_flops / t_net / 1e12,
                              "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                              "frac": mlp_flops / t_net / 1e12 / pk["bf16_tflops"],
@@ -999,7 +1046,7 @@ def _lib_check(status, what):
     _lib.check(status, what)
 
 
-def reference_library_svd(dev, st, A0, Ah, nmat, sample):
+def reference_library_svd(dev, st, A0, Ah, nmat, sample, S_ours):
     """Svd<float>::factorise: a host loop of cusolverDnSgesvd('N', 'A') over the
     matrices; timed on the first `sample` matrices and scaled (the loop's cost
     is linear in the matrix count)."""
@@ -1007,6 +1054,7 @@ def reference_library_svd(dev, st, A0, Ah, nmat, sample):
     from oracle import oracle as O
 
     R = RefLib(st)
+    sample = min(sample, A0.shape[0])
     lwork = R.L.refp_sgesvd_lwork(nmat, nmat)
     assert lwork >= 0
     work = torch.empty(max(lwork, 1), dtype=torch.float32, device=dev)
@@ -1028,8 +1076,10 @@ def reference_library_svd(dev, st, A0, Ah, nmat, sample):
     t = e[0].elapsed_time(e[1]) / 1e3
     So = O.gesvj(Ah[:min(sample, 64)], tol=1e-12)["S"]
     err = rel_err(S.cpu().numpy().reshape(sample, nmat)[:len(So)][:, None, :], So[:, None, :])
+    vs_ref = rel_err_t(S_ours[:sample], S.reshape(sample, nmat), sample)
     return {"value": sample / t, "unit": "matrices/s", "sample": sample, "ms_for_sample": t * 1e3,
             "max_rel_err_vs_fp64": {"sigma": err},
+            "ours_max_rel_err_vs_reference_output": {"sigma": vs_ref},
             "calls": f"host loop of cusolverDnSgesvd('N','A'), {sample} calls timed, scaled linearly"}
 
 
@@ -1080,7 +1130,7 @@ def run_ours_d1(args, dev, st, L, rank, world, dist):
     from gputils_gb300 import workloads, _lib
     from oracle import oracle as O
 
-    M, b = workloads.d1_cholesky()
+    M, b = workloads.d1_cholesky(k=_k(4096, args))
     k, n = M.shape[0], M.shape[1]
     nsteps = args.warmup + args.steps
     Ms = [to_dev(M, dev) for _ in range(nsteps)]
@@ -1136,6 +1186,7 @@ def run_ours_d1(args, dev, st, L, rank, world, dist):
             xr = from_dev(br, k, n, 1)
             reflib = {"value": k / (sum(tt) / len(tt)), "unit": "matrices/s", "ms": sum(tt) / len(tt) * 1e3,
                       "max_rel_err_vs_fp64": {"x": rel_err(xr[idx], xo)},
+                      "ours_max_rel_err_vs_reference_output": {"x": rel_err_t(bs[args.warmup], br, k)},
                       "calls": "cusolverDnSpotrfBatched + cusolverDnSpotrsBatched (nrhs = 1)"}
         except Exception as exc:
             reflib = {"unavailable": f"{type(exc).__name__}: {exc}"}
@@ -1155,17 +1206,67 @@ def run_ours_d1(args, dev, st, L, rank, world, dist):
     }
 
 
-def print_peaks():
-    from gputils_gb300 import build, _lib
+def _probe_lib():
+    from gputils_gb300 import build
 
-    build.build_lib()
-    L = _lib.lib()
+    if not os.path.exists(build.PROBE_LIB):
+        build.build_probe()
+    L = C.CDLL(build.PROBE_LIB)
+    L.peak_fma_throughput.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    return L
+
+
+def fp32_peak():
+    """Measure the FP32 FFMA rate once (about 0.1 s of FMA chains on every SM,
+    best of three) while sampling the SM clock; sets FP32_PEAK."""
+    import torch
+
+    L = _probe_lib()
+    rates = []
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(3):
+            g, ms = C.c_double(), C.c_double()
+            assert L.peak_fma_throughput(32, 20000, C.byref(g), C.byref(ms)) == 0
+            rates.append(g.value / 1e3)
+    ck = clk.summary()
+    FP32_PEAK.update(tflops=max(rates), sm_mhz=ck.get("sm_mhz"),
+                     source=f"FMA probe measured at bench start ({max(rates):.2f} TFLOP/s at "
+                            f"{ck.get('sm_mhz')} MHz SM clock)")
+    return FP32_PEAK
+
+
+def print_peaks():
+    import torch
+
+    torch.cuda.init()
+    L = _probe_lib()
     out = {}
     for prec, iters in ((32, 20000), (64, 200)):
         g, ms = C.c_double(), C.c_double()
-        _lib.check(L.gbla_diag_fma_throughput(prec, iters, C.byref(g), C.byref(ms)), "diag")
+        assert L.peak_fma_throughput(prec, iters, C.byref(g), C.byref(ms)) == 0
         out[f"fp{prec}_fma_tflops"] = g.value / 1e3
     print(json.dumps(out), flush=True)
+
+
+SUMMARY_KEYS = ("value", "unit", "ms_per_step", "config", "launch_config", "roofline", "roofline_network",
+                "split_ms", "max_rel_err_vs_fp64", "sweeps", "cold", "warm_over_cold", "training", "e2e",
+                "gpu_launches", "clocks", "reference_library", "cpu_baseline")
+
+
+def workload_summary(line):
+    """The fields of one workload's line kept in the default line's `workloads`
+    object, plus the ratio to the reference library path on the same GPU."""
+    out = {k: line[k] for k in SUMMARY_KEYS if k in line}
+    ref = line.get("reference_library") or {}
+    if isinstance(ref, dict) and ref.get("value"):
+        out["vs_reference_library"] = line["value"] / ref["value"]
+        if isinstance(line.get("cold"), dict):
+            out["cold"]["vs_reference_library"] = line["cold"]["value"] / ref["value"]
+    return out
+
+
+# the other configurations, run after the headline one in the default line
+OTHER_WORKLOADS = (("d1", "f32"), ("d3_f32", "f32"), ("d3_f64", "f64"), ("d4", "f32"), ("d5", "f32"))
 
 
 def main(argv=None):
@@ -1185,14 +1286,30 @@ def main(argv=None):
     torch.cuda.set_device(dev)
     if rank == 0:
         build.build_lib()
+        build.build_probe()
     if world > 1:
         dist.barrier()
     L = _lib.lib()
     st = torch.cuda.current_stream().cuda_stream
+    fp32_peak()
     runners = {"d1": run_ours_d1, "d2": run_ours_d2, "d3": run_ours_d3, "d4": run_ours_svd, "d5": run_ours_d5}
     line = runners[args.workload](args, dev, st, L, rank, world, dist)
     cpu = None if args.no_cpu_baseline or rank != 0 else CPU_BASELINES[args.workload](args.cpu_seconds, args)
     line["cpu_baseline"] = cpu
+    line["fp32_peak"] = dict(FP32_PEAK)
+    if args.workload == "d2" and not args.no_workloads:
+        # every other configuration of the metric, measured in the same run
+        subs = {}
+        for name, dt in OTHER_WORKLOADS:
+            sub = argparse.Namespace(**vars(args))
+            sub.workload, sub.dtype = name.split("_")[0], dt
+            sub.cpu_seconds = min(args.cpu_seconds, 3.0)
+            r = runners[sub.workload](sub, dev, st, L, rank, world, dist)
+            r["cpu_baseline"] = None if args.no_cpu_baseline or rank != 0 else \
+                CPU_BASELINES[sub.workload](sub.cpu_seconds, sub)
+            subs[name] = workload_summary(r)
+            torch.cuda.empty_cache()
+        line["workloads"] = subs
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -91,6 +91,24 @@ def build_baseline(verbose: bool = False) -> str:
     return BASELINE_LIB
 
 
+PROBE_SRC = os.path.join(ROOT, "baseline", "peak_probe.cu")
+PROBE_LIB = os.path.join(ROOT, "baseline", "libpeak_probe.so")
+
+
+def build_probe(verbose: bool = False) -> str:
+    """libpeak_probe.so: the FMA throughput probe bench.py uses for the
+    CUDA-core roofline denominators (bench-only, not part of libgbla.so)."""
+    if _stale(PROBE_LIB, [PROBE_SRC]):
+        cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", PROBE_SRC, "-o", PROBE_LIB]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"probe build failed:\n{r.stdout}\n{r.stderr}")
+    return PROBE_LIB
+
+
 if __name__ == "__main__":
     print(build_lib(verbose=True))
     print(build_baseline(verbose=True))
+    print(build_probe(verbose=True))

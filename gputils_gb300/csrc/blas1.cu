@@ -139,7 +139,7 @@ __global__ void k_givens_coeffs(const T *__restrict__ A, int64_t ld, int i, int 
 // Pass 1: a fixed number of blocks (depending only on len) each reduce a
 // grid-strided slice into one partial; pass 2: one block reduces the
 // partials in a fixed order.  The result is therefore bitwise reproducible.
-enum RedOp { RED_DOT = 0, RED_SQ = 1, RED_ABS = 2, RED_AMAX = 3, RED_AMIN = 4 };
+enum RedOp { RED_DOT = 0, RED_ABS = 2, RED_AMAX = 3, RED_AMIN = 4 };
 constexpr int RED_THREADS = 256;
 constexpr int RED_MAX_BLOCKS = 1024;
 
@@ -181,7 +181,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_pass1(int64_t len, const
         T v = x[i];
         T t;
         if (OP == RED_DOT) t = v * y[i];
-        else if (OP == RED_SQ) t = v * v;
         else t = v < T(0) ? -v : v;
         acc = red_combine<T, OP>(acc, t);
     }
@@ -194,7 +193,97 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_pass2(int nparts, const 
     T acc = red_identity<T, OP>();
     for (int i = threadIdx.x; i < nparts; i += RED_THREADS) acc = red_combine<T, OP>(acc, partials[i]);
     acc = block_reduce<T, OP>(acc);
-    if (threadIdx.x == 0) *result = (OP == RED_SQ) ? dev_sqrt<T>(acc) : acc;
+    if (threadIdx.x == 0) *result = acc;
+}
+
+// ------------------------------------------------------------------ nrm2
+// Euclidean norm without overflow or underflow, after Blue's three-
+// accumulator method (J. L. Blue, "A portable Fortran program to find the
+// Euclidean norm of a vector", ACM TOMS 4(1), 1978): entries of mid-range
+// magnitude are squared as they are; large entries are scaled down by a power
+// of two and small ones scaled up before squaring, each into its own sum, so
+// no entry needs a division or a running rescale.  The thresholds leave every
+// square (and any sum of up to 2^26 of them) inside the exponent range:
+//   float : |x| > 2^50 -> (x 2^-76)^2, |x| < 2^-60 -> (x 2^80)^2
+//   double: |x| > 2^480 -> (x 2^-600)^2, |x| < 2^-500 -> (x 2^600)^2
+// Pass 1 writes the three sums of each block (partials[3 b + {0,1,2}] = small,
+// mid, big); pass 2 adds them per class in a fixed order and combines the
+// classes once.  Powers of two are exact, so the scaling adds no rounding.
+template <typename T> struct Blue;
+template <> struct Blue<float> {
+    static constexpr float tbig = 0x1p50f, tsml = 0x1p-60f, sbig = 0x1p-76f, ssml = 0x1p80f;
+    static constexpr float ibig = 0x1p76f, isml = 0x1p-80f;
+};
+template <> struct Blue<double> {
+    static constexpr double tbig = 0x1p480, tsml = 0x1p-500, sbig = 0x1p-600, ssml = 0x1p600;
+    static constexpr double ibig = 0x1p600, isml = 0x1p-600;
+};
+
+template <typename T>
+__device__ __forceinline__ void blue_add(T v, T &sml, T &med, T &big) {
+    const T a = fabs(v);
+    if (a > Blue<T>::tbig) {
+        const T s = a * Blue<T>::sbig;
+        big = fma(s, s, big);
+    } else if (a < Blue<T>::tsml) {
+        const T s = a * Blue<T>::ssml;
+        sml = fma(s, s, sml);
+    } else {
+        med = fma(a, a, med);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T block_sum(T v) {
+    return block_reduce<T, RED_DOT>(v);  // RED_DOT combines by addition
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_nrm2_pass1(int64_t len, const T *__restrict__ x, T *partials) {
+    T sml = T(0), med = T(0), big = T(0);
+    for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < len; i += (int64_t)gridDim.x * RED_THREADS)
+        blue_add<T>(x[i], sml, med, big);
+    sml = block_sum<T>(sml);
+    __syncthreads();
+    med = block_sum<T>(med);
+    __syncthreads();
+    big = block_sum<T>(big);
+    if (threadIdx.x == 0) {
+        partials[3 * blockIdx.x + 0] = sml;
+        partials[3 * blockIdx.x + 1] = med;
+        partials[3 * blockIdx.x + 2] = big;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_nrm2_pass2(int nparts, const T *partials, T *result) {
+    T sml = T(0), med = T(0), big = T(0);
+    for (int i = threadIdx.x; i < nparts; i += RED_THREADS) {
+        sml += partials[3 * i + 0];
+        med += partials[3 * i + 1];
+        big += partials[3 * i + 2];
+    }
+    sml = block_sum<T>(sml);
+    __syncthreads();
+    med = block_sum<T>(med);
+    __syncthreads();
+    big = block_sum<T>(big);
+    if (threadIdx.x == 0) {
+        T r;
+        if (big > T(0)) {
+            // mid-range squares are negligible beside a big entry unless the
+            // sum is finite: fold them in at the big scale (no overflow: the
+            // scaled mid sum is tiny)
+            r = Blue<T>::ibig * dev_sqrt<T>(big + (med * Blue<T>::sbig) * Blue<T>::sbig);
+        } else if (med > T(0)) {
+            // small squares folded in at the mid scale; they matter only when
+            // the mid sum is itself near the small range
+            r = dev_sqrt<T>(med + (sml * Blue<T>::isml) * Blue<T>::isml);
+        } else {
+            r = Blue<T>::isml * dev_sqrt<T>(sml);
+        }
+        *result = r;
+    }
 }
 
 template <typename T, int OP>
@@ -209,6 +298,21 @@ static gbla_status reduce(int64_t len, const T *x, const T *y, T *result, void *
     gbla_status s = launch_status();
     if (s != GBLA_SUCCESS) return s;
     k_reduce_pass2<T, OP><<<1, RED_THREADS, 0, st>>>((int)nb, parts, result);
+    return launch_status();
+}
+
+template <typename T>
+static gbla_status nrm2(int64_t len, const T *x, T *result, void *ws, cudaStream_t st) {
+    if (len < 0 || !result || !ws) return GBLA_INVALID_VALUE;
+    if (len > 0 && !x) return GBLA_INVALID_VALUE;
+    int64_t nb = (len + RED_THREADS * 4 - 1) / (RED_THREADS * 4);
+    if (nb < 1) nb = 1;
+    if (nb > RED_MAX_BLOCKS) nb = RED_MAX_BLOCKS;
+    T *parts = reinterpret_cast<T *>(ws);
+    k_nrm2_pass1<T><<<(int)nb, RED_THREADS, 0, st>>>(len, x, parts);
+    gbla_status s = launch_status();
+    if (s != GBLA_SUCCESS) return s;
+    k_nrm2_pass2<T><<<1, RED_THREADS, 0, st>>>((int)nb, parts, result);
     return launch_status();
 }
 
@@ -233,23 +337,63 @@ static __device__ __align__(256) float g_dot_scratch[NOALLOC_DOT_PARTIALS];
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
 static std::mutex g_dot_scratch_mu;
-static float *g_dot_scratch_addr[NOALLOC_MAX_DEVICES] = {nullptr};
+struct ScratchAddr {
+    float *addr;
+    unsigned long long ctx_id;  // context the address belongs to (0: none looked up)
+};
+static ScratchAddr g_dot_scratch_addr[NOALLOC_MAX_DEVICES] = {};
 
-// Device address of g_dot_scratch on the current device; looked up on the
-// first call for each device (with that device current) and cached.
+// Unique ID of the calling thread's current CUDA context, 0 if none is current
+// or the driver cannot tell.  A device reset (cudaDeviceReset) destroys the
+// primary context, and the next runtime call creates a new one, with a new ID,
+// into which the library's module -- and g_dot_scratch -- is loaded afresh.
+// The driver entry points come through the runtime, so the library does not
+// link libcuda.
+static unsigned long long current_context_id() {
+    using GetCurrent = int (*)(void **);
+    using GetId = int (*)(void *, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    });
+    if (!get_current || !get_id) return 0;
+    void *ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return 0;
+    unsigned long long id = 0;
+    return get_id(ctx, &id) == 0 ? id : 0;
+}
+
+// Device address of g_dot_scratch on the current device.  Looked up with
+// cudaGetSymbolAddress on the first call for each device (with that device
+// current) and cached together with the ID of the context it belongs to; a
+// call in another context of that device (after a device reset) looks it up
+// again instead of using an address of a destroyed context.
 static gbla_status dot_scratch_address(float **out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return from_cuda(e);
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return GBLA_NOT_SUPPORTED;
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lock(g_dot_scratch_mu);
-    if (!g_dot_scratch_addr[dev]) {
+    ScratchAddr &c = g_dot_scratch_addr[dev];
+    if (!c.addr || ctx == 0 || c.ctx_id != ctx) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_dot_scratch);
         if (e != cudaSuccess) return from_cuda(e);
-        g_dot_scratch_addr[dev] = static_cast<float *>(p);
+        c.addr = static_cast<float *>(p);
+        c.ctx_id = current_context_id();  // the lookup has made the device's context current
     }
-    *out = g_dot_scratch_addr[dev];
+    *out = c.addr;
     return GBLA_SUCCESS;
 }
 
@@ -284,15 +428,14 @@ GBLA_API gbla_status gbla_dcopy_rows(int m, int n, int r0, int nr, const double 
                                      cudaStream_t st) {
     return copy_rows<double>(m, n, r0, nr, A, out, st);
 }
-GBLA_API size_t gbla_reduce_workspace_bytes(void) { return RED_MAX_BLOCKS * sizeof(double); }
+// three partial sums per pass-1 block (nrm2), in the widest type
+GBLA_API size_t gbla_reduce_workspace_bytes(void) { return 3 * RED_MAX_BLOCKS * sizeof(double); }
 
 #define GBLA_RED(NAME, T, OP, HASY)                                                                    \
     GBLA_API gbla_status NAME(int64_t len, const T *x, HASY T *result, void *ws, cudaStream_t st) {   \
         return reduce<T, OP>(len, x, YARG, result, ws, st);                                            \
     }
 #define YARG nullptr
-GBLA_RED(gbla_snrm2, float, RED_SQ, )
-GBLA_RED(gbla_dnrm2, double, RED_SQ, )
 GBLA_RED(gbla_sasum, float, RED_ABS, )
 GBLA_RED(gbla_dasum, double, RED_ABS, )
 GBLA_RED(gbla_samax, float, RED_AMAX, )
@@ -300,6 +443,12 @@ GBLA_RED(gbla_damax, double, RED_AMAX, )
 GBLA_RED(gbla_samin, float, RED_AMIN, )
 GBLA_RED(gbla_damin, double, RED_AMIN, )
 #undef YARG
+GBLA_API gbla_status gbla_snrm2(int64_t len, const float *x, float *result, void *ws, cudaStream_t st) {
+    return nrm2<float>(len, x, result, ws, st);
+}
+GBLA_API gbla_status gbla_dnrm2(int64_t len, const double *x, double *result, void *ws, cudaStream_t st) {
+    return nrm2<double>(len, x, result, ws, st);
+}
 GBLA_API gbla_status gbla_sdot(int64_t len, const float *x, const float *y, float *result, void *ws,
                                cudaStream_t st) {
     return reduce<float, RED_DOT>(len, x, y, result, ws, st);

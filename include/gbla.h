@@ -312,7 +312,9 @@ gbla_status gbla_dscal(int64_t len, double alpha, double *x, cudaStream_t stream
  * The scalar result is written to the device pointer `result`; `workspace`
  * must hold gbla_reduce_workspace_bytes() bytes.
  *   dot  : sum x_i y_i          replaces cublas<t>dot   (include/tensor.cuh:968-992)
- *   nrm2 : sqrt(sum x_i^2)      replaces cublas<t>nrm2  (include/tensor.cuh:994-1010)
+ *   nrm2 : sqrt(sum x_i^2)      replaces cublas<t>nrm2  (include/tensor.cuh:994-1010); entries are
+ *          scaled by powers of two into three magnitude classes before squaring (Blue's method),
+ *          so the result neither overflows nor underflows where the norm itself is representable
  *   asum : sum |x_i|            replaces cublas<t>asum  (include/tensor.cuh:1012-1028)
  *   amax : max |x_i|            replaces cublasI<t>amax + element read (include/tensor.cuh:1030-1050)
  *   amin : min |x_i|            replaces cublasI<t>amin + element read (include/tensor.cuh:1052-1072) */
@@ -339,7 +341,9 @@ gbla_status gbla_damin(int64_t len, const double *x, double *result, void *works
  * keeps it until the process exits).  Same kernels, block count and result
  * as gbla_sdot.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  All calls share the array, so calls that
+ * call before any stream capture.  The address is cached with the ID of the
+ * device's context; after a device reset the next call looks it up again in
+ * the new context (again outside capture).  All calls share the array, so calls that
  * overlap on the GPU (other streams, other host threads) race; serialise them.
  * Returns GBLA_WORKSPACE_TOO_SMALL if a length would need more than 1024
  * partial sums (none does with the current block count).  No counterpart in
@@ -464,12 +468,6 @@ gbla_status gbla_sgesvj_warm_batched(int m, int n, const float *A, int64_t strid
                                      float *Vt, int64_t strideVt, float *U, int64_t strideU, const float *V0,
                                      int64_t strideV0, int warm_budget, float tol, int max_sweeps, int *info,
                                      int *sweeps, int *fallback, int batch, cudaStream_t stream);
-
-/* -------------------------------------------------------- diagnostics */
-/* Measured FMA throughput of the device (precision 32 or 64), in GFLOP/s,
- * from a register-resident FMA probe on every SM.  Allocates and
- * synchronises; for roofline denominators only, never on a hot path. */
-gbla_status gbla_diag_fma_throughput(int precision, int iters, double *gflops, double *ms);
 
 #ifdef __cplusplus
 }

@@ -474,7 +474,7 @@ template <typename T> static void qrLS(T eps) {
     Ax -= b;
     EXPECT_NEAR(Ax.normF(), golden::qr_ls_residual, eps);
 }
-TEST(qrLeastSquares) { qrLS<float>(PRECISION_LOW * 10); qrLS<double>(PRECISION_HIGH); }
+TEST(qrLeastSquares) { qrLS<float>(PRECISION_LOW); qrLS<double>(PRECISION_HIGH); }
 
 // ---------------------------------------------------------------- Nullspace
 template <typename T> static void nullspaceTensor(T eps) {

@@ -92,6 +92,57 @@ def test_reductions_random_and_deterministic(gbla_lib, cuda, length):
     assert abs(rs.item() - np.linalg.norm(x.astype(np.float32).astype(np.float64))) < 1e-5 * np.sqrt(length)
 
 
+def _norm_exact(x):
+    """Euclidean norm in FP64 (float data) or through a power-of-two rescale
+    (double data near the ends of the exponent range)."""
+    x = np.asarray(x, dtype=np.float64)
+    amax = np.abs(x).max()
+    if amax == 0:
+        return 0.0
+    e = np.frexp(amax)[1]
+    return float(np.ldexp(np.linalg.norm(np.ldexp(x, -e)), e))
+
+
+@pytest.mark.parametrize("dt,scale", [(np.float32, 1e30), (np.float32, 1e-30), (np.float32, 1e19),
+                                      (np.float32, 1e-20), (np.float64, 1e300), (np.float64, 1e-300),
+                                      (np.float64, 1e160), (np.float64, 1e-160)])
+@pytest.mark.parametrize("length", [7, 100_003])
+def test_nrm2_extreme_magnitudes(gbla_lib, cuda, dt, scale, length):
+    """nrm2 neither overflows nor underflows where the norm is representable
+    (a plain sum of squares returns inf above ~1.8e19 and 0 below ~1e-23 in
+    float, inf above ~1.3e154 and 0 below ~1.5e-162 in double)."""
+    import torch
+    rng = np.random.default_rng(length)
+    x = (rng.standard_normal(length) * scale).astype(dt)
+    x[length // 2] = dt(scale * 3.0)  # one entry well above the others
+    xd = torch.tensor(x).cuda()
+    ws = torch.empty(gbla_lib.gbla_reduce_workspace_bytes(), dtype=torch.uint8, device="cuda")
+    res = torch.zeros(1, dtype=xd.dtype, device="cuda")
+    assert getattr(gbla_lib, f"gbla_{PFX[dt]}nrm2")(length, ptr(xd), ptr(res), ptr(ws), stream()) == 0
+    got, want = res.item(), _norm_exact(x)
+    assert np.isfinite(got) and got > 0
+    tol = (1e-5 if dt == np.float32 else 1e-12) * max(1.0, np.sqrt(length) / 10)
+    assert abs(got - want) <= tol * want, (got, want)
+
+
+def test_nrm2_mixed_magnitudes(gbla_lib, cuda):
+    """Entries from all three magnitude classes in one vector, float and double."""
+    import torch
+    ws = torch.empty(gbla_lib.gbla_reduce_workspace_bytes(), dtype=torch.uint8, device="cuda")
+    for dt, vals in ((np.float32, [3e20, 4e20, 1.0, 2.0, 1e-25, 5e-30]),
+                     (np.float64, [3e200, 4e200, 1.0, 1e-200, 2e-300])):
+        x = np.array(vals * 1000, dtype=dt)
+        xd = torch.tensor(x).cuda()
+        res = torch.zeros(1, dtype=xd.dtype, device="cuda")
+        assert getattr(gbla_lib, f"gbla_{PFX[dt]}nrm2")(len(x), ptr(xd), ptr(res), ptr(ws), stream()) == 0
+        want = _norm_exact(x)
+        assert abs(res.item() - want) <= (1e-6 if dt == np.float32 else 1e-14) * want * 10
+    zero = torch.zeros(5, dtype=torch.float32, device="cuda")
+    res = torch.full((1,), 7.0, dtype=torch.float32, device="cuda")
+    assert gbla_lib.gbla_snrm2(5, ptr(zero), ptr(res), ptr(ws), stream()) == 0
+    assert res.item() == 0.0
+
+
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_copy_rows_golden(gbla_lib, cuda, dt):
     import torch

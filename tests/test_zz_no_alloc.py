@@ -39,7 +39,8 @@ def test_noalloc_dot_matches_workspace_dot_on_two_calls(gbla_lib, cuda):
         assert gbla_lib.gbla_sdot_noalloc(length, x.data_ptr(), y.data_ptr(), out.data_ptr(), stream) == 0
         got = out.item()
         want = _dot_with_workspace(gbla_lib, x, y, stream)
-        # same kernels and block count: expected bit-identical; the suite's float tolerance bounds it
+        # same kernels, block count and summation order as gbla_sdot: identical bits
+        assert np.float32(got).tobytes() == np.float32(want).tobytes(), (length, got, want)
         assert abs(got - want) <= 1e-6 * max(1.0, abs(want)), (length, got, want)
         exact = float(x.double().cpu().numpy() @ y.double().cpu().numpy())
         assert abs(got - exact) <= 1e-4 * np.sqrt(length), (length, got, exact)
