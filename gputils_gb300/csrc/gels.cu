@@ -10,7 +10,9 @@ static gbla_status gels_cta_launch(int m, int n, int nrhs, float *A, int64_t sA,
     if (m < 0 || n < 0 || nrhs < 0 || batch < 0 || refine < 0 || m < n) return GBLA_INVALID_VALUE;
     if (batch == 0 || n == 0) return GBLA_SUCCESS;
     if (!A || sA < (int64_t)m * n || (nrhs > 0 && (!B || sB < (int64_t)m * nrhs))) return GBLA_INVALID_VALUE;
-    if (m > 128 || n > 32) return GBLA_NOT_SUPPORTED;
+    if (m > 128 || n > 32)
+        return qr_big_launch<float>(m, n, nrhs, A, sA, B, sB, nullptr, 0, info, QR_WRITE_FACTORS | QR_SOLVE, refine,
+                                    batch, st);
     const int R = (m + 31) / 32;
     // factors, two Householder vectors, taus, and the original A when refining
     const size_t smem = sizeof(float) * ((size_t)32 * (32 * R + 1) + (refine > 0 ? 32 * 32 * R : 0) + 2 * 32 * R + 32);

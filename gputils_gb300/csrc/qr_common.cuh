@@ -23,11 +23,10 @@
 // The original A is kept in shared memory for the residuals.
 #pragma once
 #include "common.cuh"
+#include "qr_big.cuh"
 #include "xprec.cuh"
 
 namespace gbla {
-
-enum QrFlags { QR_WRITE_FACTORS = 1, QR_WRITE_TAU = 2, QR_SOLVE = 4 };
 
 // ------------------------------------------------------------ butterfly
 // On entry p[j] is this lane's partial for slot j (32 slots); on exit the
@@ -728,8 +727,8 @@ static inline gbla_status qr_launch(int m, int n, int nrhs, T *A, int64_t sA, T 
     if (!A || sA < (int64_t)m * n) return GBLA_INVALID_VALUE;
     if ((flags & QR_SOLVE) && nrhs > 0 && (!B || sB < (int64_t)m * nrhs)) return GBLA_INVALID_VALUE;
     if ((flags & QR_WRITE_TAU) && (!tau || sTau < n)) return GBLA_INVALID_VALUE;
-    if (m > 128 || n > 32) return GBLA_NOT_SUPPORTED;
     if (sizeof(T) != 4) refine = 0;
+    if (m > 128 || n > 32) return qr_big_launch<T>(m, n, nrhs, A, sA, B, sB, tau, sTau, info, flags, refine, batch, st);
     const int R = (m + 31) / 32;
     // shared memory: per warp the original A (refinement only) and 32 taus
     size_t smem = (size_t)4 * ((refine > 0 ? 32 * R * 32 : 0) + 32) * sizeof(T);
@@ -771,7 +770,7 @@ static inline gbla_status ormqr_launch(int trans, int m, int nc, int k, const T 
     if (m < 0 || nc < 0 || k < 0 || k > m || batch < 0) return GBLA_INVALID_VALUE;
     if (batch == 0 || nc == 0 || k == 0 || m == 0) return GBLA_SUCCESS;
     if (!A || !tau || !Cm || sA < (int64_t)m * k || sTau < k || sC < (int64_t)m * nc) return GBLA_INVALID_VALUE;
-    if (m > 128) return GBLA_NOT_SUPPORTED;
+    if (m > 128) return ormqr_big_launch<T>(trans, m, nc, k, A, sA, tau, sTau, Cm, sC, batch, st);
     const unsigned grid = (unsigned)((batch + 3) / 4);
     switch ((m + 31) / 32) {
         case 1: k_ormqr_warp<T, 1><<<grid, 128, 0, st>>>(trans, m, nc, k, A, sA, tau, sTau, Cm, sC, batch); break;

@@ -24,6 +24,7 @@
 // over e_0..e_{m-1}, the c-th completion column negated for odd c).
 #include <cfloat>
 #include "common.cuh"
+#include "svd_big.cuh"
 
 namespace gbla {
 
@@ -705,6 +706,10 @@ static gbla_status svd_launch(int m, int n, const T *A, int64_t sA, T *S, int64_
         SVJ_LAUNCH(128, 64)
 #undef SVJ_LAUNCH
     }
+    // wider or taller: one block per matrix, A in shared or global memory (no warm start)
+    if (!V0 && n <= SVD_BIG_MAX_N)
+        return svd_big_launch<T>(m, n, const_cast<T *>(A), sA, S, sS, Vt, sVt, U, sU, tol, max_sweeps, info, sweeps,
+                                 batch, st);
     return GBLA_NOT_SUPPORTED;
 }
 

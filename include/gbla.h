@@ -156,10 +156,13 @@ gbla_status gbla_dposv_ragged(const gbla_ragged_plan *plan, double *A, double *B
                               cudaStream_t stream);
 
 /* -------------------------------------------------------------------- QR */
-/* Householder QR of m x n matrices (m >= n, m <= 128, n <= 32): R in the
- * upper triangle, the Householder vectors below it (LAPACK dgeqrf
- * convention), tau (n per matrix, batch stride strideTau).  info[i] = j if
- * R(j-1, j-1) is exactly zero, else 0 (nullable).
+/* Householder QR of m x n matrices (any m >= n): R in the upper triangle,
+ * the Householder vectors below it (LAPACK dgeqrf convention), tau (n per
+ * matrix, batch stride strideTau).  info[i] = j if R(j-1, j-1) is exactly
+ * zero, else 0 (nullable).  m <= 128 and n <= 32 run one warp per matrix in
+ * registers; larger shapes one block per matrix, the matrix in shared memory
+ * when it fits (m n elements up to ~57k floats / ~28k doubles), else worked
+ * on in place in A.
  * Replaces cusolverDn<t>geqrf (include/tensor.cuh:1866-1889). */
 gbla_status gbla_sgeqrf_batched(int m, int n, float *A, int64_t strideA, float *tau, int64_t strideTau,
                                 int *info, int batch, cudaStream_t stream);
@@ -167,7 +170,8 @@ gbla_status gbla_dgeqrf_batched(int m, int n, double *A, int64_t strideA, double
                                 int *info, int batch, cudaStream_t stream);
 
 /* C_i <- Q_i^T C_i (trans != 0) or Q_i C_i, Q_i = H_0 ... H_{k-1} from a
- * geqrf result (A_i m x k, tau_i), C_i m x nc.  m <= 128.
+ * geqrf result (A_i m x k, tau_i), C_i m x nc.  Any m (m <= 128: one warp per
+ * matrix in registers; larger: one warp per column of C, in place).
  * Replaces cusolverDn<t>ormqr (include/tensor.cuh:1891-1927, 1946-1952). */
 gbla_status gbla_sormqr_batched(int trans, int m, int nc, int k, const float *A, int64_t strideA,
                                 const float *tau, int64_t strideTau, float *C, int64_t strideC, int batch,
@@ -185,14 +189,18 @@ gbla_status gbla_strsm_upper_batched(int n, int nc, const float *R, int64_t ldr,
 gbla_status gbla_dtrsm_upper_batched(int n, int nc, const double *R, int64_t ldr, int64_t strideR, double *B,
                                      int64_t ldb, int64_t strideB, int batch, cudaStream_t stream);
 
-/* Least squares min ||A_i x - b_i|| for each of nrhs columns (m >= n,
- * m <= 128, n <= 32): A_i is overwritten with its QR factors and rows [0, n)
- * of each B_i column with the solution (rows [n, m) hold (Q^T b)(n:m)).
- * Single precision: refine_iters steps of augmented-system refinement with
- * double-FP32 residuals recover FP64-level accuracy of x.  info as geqrf.
- * Single precision runs one block of four warps per system, on chip from
- * load to store (each warp factorises a quarter of the columns, then solves
- * one right-hand side at a time); double precision one warp per system.
+/* Least squares min ||A_i x - b_i|| for each of nrhs columns (any m >= n):
+ * A_i is overwritten with its QR factors and rows [0, n) of each B_i column
+ * with the solution (rows [n, m) hold (Q^T b)(n:m)).  Single precision:
+ * refine_iters steps of augmented-system refinement with double-FP32
+ * residuals recover FP64-level accuracy of x.  info as geqrf.
+ * m <= 128, n <= 32: single precision runs one block of four warps per
+ * system, on chip from load to store (each warp factorises a quarter of the
+ * columns, then solves one right-hand side at a time); double precision one
+ * warp per system.  Larger shapes: one block per system (the geqrf block
+ * kernel, then one warp per right-hand side); single-precision refinement
+ * needs the working copy in shared memory (m n up to ~50k) and returns
+ * GBLA_NOT_SUPPORTED beyond it (refine_iters = 0 works for any shape).
  * Replaces cublas<t>gelsBatched in DTensor::leastSquaresBatched
  * (include/tensor.cuh:1340-1394), which allows nrhs = 1 only. */
 gbla_status gbla_sgels_batched(int m, int n, int nrhs, float *A, int64_t strideA, float *B, int64_t strideB,
@@ -245,7 +253,7 @@ gbla_status gbla_sgels_batched_host(gbla_stream_pipeline *pipeline, int m, int n
 
 /* ------------------------------------------------------------------- SVD */
 /* One-sided (Hestenes) Jacobi SVD A_i = U_i diag(S_i) Vt_i of m x n matrices
- * (m >= n; n <= 64, m <= 128), in the precision of the data (s: FP32,
+ * (any m >= n, n <= 128; warm start V0: n <= 64, m <= 128), in the precision of the data (s: FP32,
  * d: FP64; tol' below uses the unit roundoff of that precision).
  * S_i: n singular values, descending.  Vt_i: n x n (= V^T, as Svd::
  * rightSingularVectors returns).  U_i: m x m, nullable (computeU = false).
@@ -275,7 +283,7 @@ gbla_status gbla_srank_batched(int len, const float *S, int64_t strideS, float e
 gbla_status gbla_drank_batched(int len, const double *S, int64_t strideS, double eps, unsigned int *rank,
                                int batch, cudaStream_t stream);
 
-/* Null space of square or fat m x n matrices (1 <= m <= n <= 64): N_i (n x n)
+/* Null space of square or fat m x n matrices (1 <= m <= n, m <= 128): N_i (n x n)
  * holds an orthonormal basis of ker(A_i) in its first nullity_i columns
  * (zero-padded), P_i = N_i N_i^T (n x n).  Singular values <= eps, or
  * below the FP32 noise level n * FLT_EPSILON * sigma_max, count as zero.  nullity (nullable) receives n - rank.  info as gesvj (nullable).
