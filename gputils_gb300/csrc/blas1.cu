@@ -135,6 +135,75 @@ __global__ void k_givens_coeffs(const T *__restrict__ A, int64_t ld, int i, int 
     out[2] = xk * r;
 }
 
+// ------------------------------------------------------- batched Givens
+// Rotation of two strided vectors in each of `batch` problems, each with its
+// own (c, s) read from device memory: x_b, y_b start at x + b stride, y + b
+// stride; c_b = c[b cs_stride], s_b = s[b cs_stride].
+template <typename T>
+__global__ void k_rot_batched(int64_t len, T *__restrict__ x, int64_t incx, T *__restrict__ y, int64_t incy,
+                              int64_t stride, const T *__restrict__ c, const T *__restrict__ s, int64_t cs_stride,
+                              int64_t total) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = e / len, i = e % len;
+        const T cb = c[b * cs_stride], sb = s[b * cs_stride];
+        T *xp = x + b * stride + i * incx, *yp = y + b * stride + i * incy;
+        const T xv = *xp, yv = *yp;
+        *xp = cb * xv + sb * yv;
+        *yp = cb * yv - sb * xv;
+    }
+}
+
+// GivensAnnihilator::annihilate on every matrix of a batch in one launch: one
+// warp per matrix reads A(i, j) and A(k, j), forms r = 1 / hypot, c = A(i, j) r
+// and s = A(k, j) r (the reference's k_givensAnnihilateRHypot), then rotates
+// rows i and k across all n columns (cublas<t>rot with c and -s = s), which
+// zeroes A(k, j).  coeffs (nullable) receives (r, c, s) per matrix.
+template <typename T>
+__global__ void __launch_bounds__(256) k_givens_annihilate_batched(int m, int n, T *__restrict__ A, int64_t sA, int i,
+                                                                   int k, int j, T *__restrict__ coeffs, int batch) {
+    const int lane = threadIdx.x & 31;
+    const int64_t mat = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (mat >= batch) return;  // whole warps leave together
+    T *a = A + mat * sA;
+    const T xij = a[(int64_t)j * m + i], xkj = a[(int64_t)j * m + k];
+    const T r = rhypot(xij, xkj);
+    const T c = xij * r, s = xkj * r;
+    __syncwarp();  // every lane has read column j before any lane rotates it
+    for (int col = lane; col < n; col += 32) {
+        const T xv = a[(int64_t)col * m + i], yv = a[(int64_t)col * m + k];
+        a[(int64_t)col * m + i] = c * xv + s * yv;
+        a[(int64_t)col * m + k] = c * yv - s * xv;
+    }
+    if (coeffs && lane == 0) {
+        coeffs[3 * mat] = r;
+        coeffs[3 * mat + 1] = c;
+        coeffs[3 * mat + 2] = s;
+    }
+}
+
+template <typename T>
+static gbla_status rot_batched(int64_t len, T *x, int64_t incx, T *y, int64_t incy, int64_t stride, const T *c,
+                               const T *s, int64_t cs_stride, int batch, cudaStream_t st) {
+    if (len < 0 || incx < 1 || incy < 1 || batch < 0 || stride < 0 || cs_stride < 0) return GBLA_INVALID_VALUE;
+    if (len == 0 || batch == 0) return GBLA_SUCCESS;
+    if (!x || !y || !c || !s) return GBLA_INVALID_VALUE;
+    const int64_t total = len * batch;
+    k_rot_batched<T><<<stream_grid(total), 256, 0, st>>>(len, x, incx, y, incy, stride, c, s, cs_stride, total);
+    return launch_status();
+}
+
+template <typename T>
+static gbla_status givens_annihilate_batched(int m, int n, T *A, int64_t sA, int i, int k, int j, T *coeffs, int batch,
+                                             cudaStream_t st) {
+    if (m < 0 || n < 0 || batch < 0 || sA < (int64_t)m * n) return GBLA_INVALID_VALUE;
+    if (i < 0 || k < 0 || j < 0 || i >= m || k >= m || j >= n || i == k) return GBLA_INVALID_VALUE;
+    if (batch == 0) return GBLA_SUCCESS;
+    if (!A) return GBLA_INVALID_VALUE;
+    const int64_t blocks = ((int64_t)batch * 32 + 255) / 256;
+    k_givens_annihilate_batched<T><<<(unsigned)blocks, 256, 0, st>>>(m, n, A, sA, i, k, j, coeffs, batch);
+    return launch_status();
+}
+
 // --------------------------------------------------------------- reductions
 // Pass 1: a fixed number of blocks (depending only on len) each reduce a
 // grid-strided slice into one partial; pass 2: one block reduces the
@@ -494,6 +563,23 @@ GBLA_API gbla_status gbla_drot_dev(int64_t len, double *x, int64_t incx, double 
                                    const double *s, cudaStream_t st) {
     if (!c || !s) return GBLA_INVALID_VALUE;
     return rot<double>(len, x, incx, y, incy, 0.0, 0.0, c, s, st);
+}
+GBLA_API gbla_status gbla_srot_batched(int64_t len, float *x, int64_t incx, float *y, int64_t incy, int64_t stride,
+                                       const float *c, const float *s, int64_t cs_stride, int batch, cudaStream_t st) {
+    return rot_batched<float>(len, x, incx, y, incy, stride, c, s, cs_stride, batch, st);
+}
+GBLA_API gbla_status gbla_drot_batched(int64_t len, double *x, int64_t incx, double *y, int64_t incy, int64_t stride,
+                                       const double *c, const double *s, int64_t cs_stride, int batch,
+                                       cudaStream_t st) {
+    return rot_batched<double>(len, x, incx, y, incy, stride, c, s, cs_stride, batch, st);
+}
+GBLA_API gbla_status gbla_sgivens_annihilate_batched(int m, int n, float *A, int64_t sA, int i, int k, int j,
+                                                     float *coeffs, int batch, cudaStream_t st) {
+    return givens_annihilate_batched<float>(m, n, A, sA, i, k, j, coeffs, batch, st);
+}
+GBLA_API gbla_status gbla_dgivens_annihilate_batched(int m, int n, double *A, int64_t sA, int i, int k, int j,
+                                                     double *coeffs, int batch, cudaStream_t st) {
+    return givens_annihilate_batched<double>(m, n, A, sA, i, k, j, coeffs, batch, st);
 }
 GBLA_API gbla_status gbla_sgivens_coeffs(const float *A, int64_t ld, int i, int k, int j, float *out,
                                          cudaStream_t st) {

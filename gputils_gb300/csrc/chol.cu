@@ -104,24 +104,35 @@ __global__ void __launch_bounds__(128, 1) k_chol_lanerow(int n, int nrhs, T *__r
 }
 
 // ------------------------------------------------------------------ CTA kernel
-template <typename T>
+// Per-warp solve columns of the CTA kernel: x, plus a residual column when
+// refinement runs on n > 128 (the n <= 128 refinement keeps it in registers).
+__host__ __device__ inline int cta_xcols(int n, int refine) { return (refine > 0 && n > 128) ? 2 : 1; }
+
+// SMEM: the lower triangle is worked on in shared memory (odd leading
+// dimension); otherwise (n beyond shared memory) in place in A, leading
+// dimension n -- the factor overwrites A in any case, and without a copy of
+// the original there is no refinement (the launcher refuses it).
+template <typename T, bool SMEM>
 __global__ void __launch_bounds__(CTA_THREADS, 1) k_chol_cta(int n, int nrhs, T *__restrict__ A, int64_t sA,
                                                           T *__restrict__ B, int64_t sB, int *__restrict__ info,
                                                           int mode, int refine, int batch) {
     using R = typename ResT<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *a = reinterpret_cast<T *>(smem_raw);
-    const int ld = cta_ld(n);
-    T *xs = a + (size_t)n * ld;
-    T *dinv = xs + (size_t)n * CTA_RHS_CHUNK;
+    T *as = reinterpret_cast<T *>(smem_raw);
+    const int ld = SMEM ? cta_ld(n) : n;
+    const int xcols = cta_xcols(n, refine);
+    T *xs = as + (SMEM ? (size_t)n * ld : 0);
+    T *dinv = xs + (size_t)n * CTA_RHS_CHUNK * xcols;
     __shared__ int s_fail;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     for (int64_t mat = blockIdx.x; mat < batch; mat += gridDim.x) {
         T *a_g = A + mat * sA;
+        T *a = SMEM ? as : a_g;
         // lower triangle -> shared memory (warp per column, lanes along rows)
-        for (int j = warp; j < n; j += CTA_WARPS)
-            for (int i = j + lane; i < n; i += 32) a[(int64_t)j * ld + i] = a_g[(int64_t)j * n + i];
+        if (SMEM)
+            for (int j = warp; j < n; j += CTA_WARPS)
+                for (int i = j + lane; i < n; i += 32) a[(int64_t)j * ld + i] = a_g[(int64_t)j * n + i];
         if (threadIdx.x == 0) s_fail = 0;
         __syncthreads();
 
@@ -156,11 +167,29 @@ __global__ void __launch_bounds__(CTA_THREADS, 1) k_chol_cta(int n, int nrhs, T 
             for (int c0 = 0; c0 < nrhs; c0 += CTA_RHS_CHUNK) {
                 int c = c0 + warp;
                 if (c < nrhs) {
-                    T *x = xs + (size_t)warp * n;
+                    T *x = xs + (size_t)warp * n * xcols;
                     for (int i = lane; i < n; i += 32) x[i] = b_g[(int64_t)c * n + i];
                     __syncwarp();
                     cta_solve_col<T>(a, ld, dinv, x, n, lane);
-                    if ((mode & CH_FACTOR) && refine > 0) {
+                    if (SMEM && (mode & CH_FACTOR) && refine > 0 && n > 128) {
+                        // any n: r = b - A x row by row from the original lower
+                        // triangle (A(i, j) = A(j, i) above it), in R precision
+                        T *d = x + n;
+                        for (int it = 0; it < refine; it++) {
+                            for (int i = lane; i < n; i += 32) {
+                                R acc = R(b_g[(int64_t)c * n + i]);
+                                for (int j = 0; j < n; j++) {
+                                    const T aij = i >= j ? a_g[(int64_t)j * n + i] : a_g[(int64_t)i * n + j];
+                                    acc -= R(aij) * R(x[j]);
+                                }
+                                d[i] = T(acc);
+                            }
+                            __syncwarp();
+                            cta_solve_col<T>(a, ld, dinv, d, n, lane);
+                            for (int i = lane; i < n; i += 32) x[i] += d[i];
+                            __syncwarp();
+                        }
+                    } else if (SMEM && (mode & CH_FACTOR) && refine > 0) {
                         // x is kept in T; corrections come from an R-precision residual.
                         for (int it = 0; it < refine; it++) {
                             // r = b - A x (A symmetric, lower triangle of the original in global)
@@ -219,7 +248,7 @@ __global__ void __launch_bounds__(CTA_THREADS, 1) k_chol_cta(int n, int nrhs, T 
             }
         }
         __syncthreads();
-        if (mode & CH_FACTOR) {
+        if (SMEM && (mode & CH_FACTOR)) {
             for (int j = warp; j < n; j += CTA_WARPS)
                 for (int i = j + lane; i < n; i += 32) a_g[(int64_t)j * n + i] = a[(int64_t)j * ld + i];
         }
@@ -227,16 +256,13 @@ __global__ void __launch_bounds__(CTA_THREADS, 1) k_chol_cta(int n, int nrhs, T 
     }
 }
 
-static int max_cta_n(size_t elem) {
-    // largest n whose working set fits the 227 KB opt-in shared memory
-    int n = 32;
-    while (true) {
-        size_t b = elem * ((size_t)(n + 1) * cta_ld(n + 1) + (size_t)(n + 1) * CTA_RHS_CHUNK + (n + 1)) + 16;
-        if (b > 227 * 1024) break;
-        n++;
-    }
-    return n;
+// shared memory of the CTA kernel: matrix (SMEM only), solve columns, 1 / L_kk
+template <typename T>
+static size_t chol_cta_smem(int n, int refine, bool smem_matrix) {
+    return sizeof(T) * ((smem_matrix ? (size_t)n * cta_ld(n) : 0) + (size_t)n * CTA_RHS_CHUNK * cta_xcols(n, refine) +
+                        (size_t)n) + 16;
 }
+constexpr size_t CHOL_SMEM_MAX = 226 * 1024;  // below the 227 KB opt-in (room for static shared memory)
 
 template <typename T>
 static gbla_status chol_launch(int n, int nrhs, T *A, int64_t sA, T *B, int64_t sB, int *info, int mode,
@@ -246,9 +272,6 @@ static gbla_status chol_launch(int n, int nrhs, T *A, int64_t sA, T *B, int64_t 
     if (!A || sA < (int64_t)n * n) return GBLA_INVALID_VALUE;
     if ((mode & CH_SOLVE) && (!B || sB < (int64_t)n * nrhs)) return GBLA_INVALID_VALUE;
     if ((mode & CH_SOLVE) && nrhs == 0 && !(mode & CH_FACTOR)) return GBLA_SUCCESS;
-    if (n > 128 && n > max_cta_n(sizeof(T))) return GBLA_NOT_SUPPORTED;
-    // refinement reads rows lane + 32 s for s < 4 in the CTA kernel
-    if (refine > 0 && n > 128) return GBLA_NOT_SUPPORTED;
     if (n <= 32) {
         int nb = n <= 8 ? 8 : (n <= 16 ? 16 : 32);
         int mpb = 4 * (32 / nb);
@@ -277,14 +300,22 @@ static gbla_status chol_launch(int n, int nrhs, T *A, int64_t sA, T *B, int64_t 
         if (e != cudaSuccess) return from_cuda(e);
         return launch_status();
     }
-    size_t smem = cta_smem_bytes<T>(n);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_chol_cta<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return from_cuda(e);
-    }
-    const int64_t grid = persistent_grid(reinterpret_cast<const void *>(k_chol_cta<T>), CTA_THREADS, smem, batch);
-    k_chol_cta<T><<<(unsigned)grid, CTA_THREADS, smem, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
-    return launch_status();
+    const bool fits = chol_cta_smem<T>(n, refine, true) <= CHOL_SMEM_MAX;
+    // beyond shared memory the factor is computed in place in A: the original
+    // A is gone, so there is nothing to refine against
+    if (!fits && refine > 0 && (mode & CH_FACTOR) && (mode & CH_SOLVE)) return GBLA_NOT_SUPPORTED;
+    const size_t smem = chol_cta_smem<T>(n, refine, fits);
+    if (smem > CHOL_SMEM_MAX) return GBLA_NOT_SUPPORTED;  // the solve columns alone do not fit
+    auto go = [&](auto kern) -> gbla_status {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return from_cuda(e);
+        }
+        const int64_t grid = persistent_grid(reinterpret_cast<const void *>(kern), CTA_THREADS, smem, batch);
+        kern<<<(unsigned)grid, CTA_THREADS, smem, st>>>(n, nrhs, A, sA, B, sB, info, mode, refine, batch);
+        return launch_status();
+    };
+    return fits ? go(k_chol_cta<T, true>) : go(k_chol_cta<T, false>);
 }
 
 }  // namespace gbla

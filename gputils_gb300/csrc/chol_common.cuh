@@ -93,12 +93,6 @@ constexpr int CTA_RHS_CHUNK = CTA_WARPS;  // one warp per right-hand side
 
 __host__ __device__ inline int cta_ld(int n) { return n | 1; }
 
-template <typename T>
-__host__ __device__ inline size_t cta_smem_bytes(int n) {
-    int ld = cta_ld(n);
-    return sizeof(T) * ((size_t)n * ld + (size_t)n * CTA_RHS_CHUNK + n) + 16;
-}
-
 // Solve L L^T x = b for the column x (length n, shared memory) with one warp.
 template <typename T>
 __device__ __forceinline__ void cta_solve_col(const T *__restrict__ a, int ld, const T *__restrict__ dinv,

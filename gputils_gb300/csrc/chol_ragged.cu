@@ -3,21 +3,31 @@
 //
 // The reference has no ragged API: a mixed batch is one
 // CholeskyBatchFactoriser per size and one potrs per right-hand-side column
-// (include/tensor.cuh:2100-2197).  Here a host-built plan sorts the systems:
-//   * n <= 32  : three size classes (n <= 8, 16, 32); each class runs the
-//                lane-row kernel (NB lanes per system, rows in registers,
-//                shuffles only).  Within a warp the loop bounds are the warp's
-//                largest n / nrhs; smaller systems are padded with the
-//                identity, which leaves their factor and solution unchanged.
-//   * n > 32   : one block per system, shared-memory factor, one warp per
-//                right-hand side; blocks are issued largest system first.
-// The large class is cut into buckets of similar n (each launch sizes its
-// shared memory for its own largest system, so small members of the class are
-// not run at the occupancy of n = 128), spread over forked streams.  Bucket
-// width, threads per block and whether the small classes get their own stream
-// form the plan's launch configuration; gbla_{s,d}ragged_autotune times the
-// candidates on the caller's batch and keeps the fastest.  All forks and joins
-// are event-based, so a call can be captured in a CUDA graph.
+// (include/tensor.cuh:2100-2197).  Here a host-built plan sorts the systems
+// and cuts them into tasks, and a call is ONE persistent kernel launch whose
+// blocks pull tasks from a device queue (an atomic counter; a block that finds
+// the queue empty leaves, and the last block to leave resets the counter for
+// the next call, so a call needs no memset and replays in a CUDA graph):
+//   * n > 32   : a task is a group of 1..systems_per_block systems of similar
+//                size (largest first), each worked on by threads/32/count
+//                warps in its own shared-memory slot: blocked factorisation
+//                (one warp factors an 8-column panel while the others apply
+//                the previous panel's update; a named barrier per system), one
+//                warp per right-hand side for the solves and refinement.
+//   * n <= 32  : three size classes (n <= 8, 16, 32) run the lane-row method
+//                (NB lanes per system, rows in registers, shuffles only); a
+//                task is one class's systems for every warp of the block.
+//                Within a warp the loop bounds are the warp's largest n /
+//                nrhs; smaller systems are padded with the identity, which
+//                leaves their factor and solution unchanged.
+// Tasks are queued largest first (LPT), so the queue balances the n^3 spread
+// of the work across the persistent blocks.  The launch configuration --
+// threads per block and the most large systems a block takes at once (which
+// sets its shared memory and with it the blocks per SM) -- is a plan
+// property; gbla_{s,d}ragged_autotune times every candidate on the caller's
+// batch and keeps the fastest.  Every configuration gives bit-identical
+// results: each element of each system receives its updates in the same
+// order whatever the grouping.
 //
 // Precision: the factorisation and the triangular solves run in FP32; each
 // refinement step recomputes r = b - A x from the original, full symmetric A
@@ -34,8 +44,12 @@ struct RaggedSys {
     int n, nrhs, orig, pad;
 };
 
-constexpr int RG_MAX_BUCKETS = 8;
-constexpr int RG_STREAMS = 3;  // forked streams: small classes, two for large buckets
+// A task of the persistent launch: `count` systems from sys[first] on, either
+// a group of large systems (nb == 0; `warps` warps and one shared-memory slot
+// sized for nmax each) or a chunk of one small class (nb = lanes per system).
+struct RaggedTask {
+    int first, count, nb, warps, nmax, pad;
+};
 
 struct gbla_ragged_plan {
     int device = -1;
@@ -43,28 +57,28 @@ struct gbla_ragged_plan {
     int first[4] = {0, 0, 0, 0};   // classes: NB 8, NB 16, NB 32, large
     int num[4] = {0, 0, 0, 0};
     int max_n_large = 0;
-    gbla_ragged_config cfg = {96, 256, 1};
-    // large-class buckets for cfg.bucket_width (contiguous, largest n first)
-    int nb = 0, b_first[RG_MAX_BUCKETS] = {}, b_num[RG_MAX_BUCKETS] = {}, b_nmax[RG_MAX_BUCKETS] = {};
+    gbla_ragged_config cfg = {256, 2};
+    int ntasks = 0;
+    size_t smem = 0;                     // dynamic shared memory per block for cfg
     int64_t a_extent = 0, b_extent = 0;  // arena sizes in elements
     std::vector<int> large_n;            // n of the large class, in plan order
     RaggedSys *d_sys = nullptr;
-    cudaStream_t aux[RG_STREAMS] = {};
-    cudaEvent_t fork = nullptr, join[RG_STREAMS] = {};
+    RaggedTask *d_tasks = nullptr;       // capacity: count tasks
+    int *d_ctr = nullptr;                // queue head, blocks finished
 };
 
 namespace gbla {
 
 
 // ------------------------------------------------------------ small systems
+// One warp's share of a small-class task: systems first + warp * GPW + g.
 template <typename T, int NB>
-__global__ void __launch_bounds__(128, 1)
-    k_ragged_small(const RaggedSys *__restrict__ sys, int first, int count, const T *__restrict__ A_in,
-                   T *__restrict__ A, T *__restrict__ B, int *__restrict__ info, int refine) {
+__device__ __forceinline__ void small_systems(const RaggedSys *__restrict__ sys, int first, int count, int warp,
+                                              int lane, const T *__restrict__ A_in, T *__restrict__ A,
+                                              T *__restrict__ B, int *__restrict__ info, int refine) {
     constexpr int GPW = 32 / NB;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane / NB, r = lane % NB;
-    const int local = (blockIdx.x * 4 + warp) * GPW + g;
+    const int local = warp * GPW + g;
     const bool act = local < count;
     RaggedSys s = {0, 0, 0, 0, 0, 0};
     if (act) s = sys[first + local];
@@ -135,12 +149,12 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // ------------------------------------------------------------ large systems
-template <typename T>
-__host__ __device__ inline size_t ragged_large_smem(int nmax, int warps) {
+// Shared-memory slot of one large system: two panel-row buffers (n x 8 each),
+// the FP32 factor (n x ld), 1 / L_kk (n) and the failure flag; a multiple of
+// 16 bytes so that consecutive slots stay 16-byte aligned.
+__host__ __device__ inline size_t ragged_slot_bytes(int nmax) {
     const int ld = cta_ld(nmax);
-    (void)warps;
-    // two panel-row buffers (n x 8 each, 16-byte aligned) + float factor (n x ld) + float dinv (n)
-    return sizeof(float) * ((size_t)nmax * 16 + (size_t)nmax * ld + (size_t)nmax) + 64;
+    return (sizeof(float) * ((size_t)nmax * 16 + (size_t)nmax * ld + (size_t)nmax) + 16 + 15) & ~(size_t)15;
 }
 
 // Solve L L^T x = b for one column held in registers (element lane + 32 t in
@@ -273,36 +287,39 @@ __device__ __forceinline__ T xget(const T (&x)[4], int tk, int lk) {
     return shfl(tk == 0 ? x[0] : tk == 1 ? x[1] : tk == 2 ? x[2] : x[3], lk);
 }
 
-// at least 3 blocks of 256 (6 of 128, 12 of 64, 1 of 512) per SM: register cap ~85
-template <typename T, int THREADS>
-__global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
-    k_ragged_large(const RaggedSys *__restrict__ sys, int first, int nmax, const T *__restrict__ A_in,
-                   T *__restrict__ A, T *__restrict__ B, int *__restrict__ info, int refine) {
-    constexpr int RG_LARGE_WARPS = THREADS / 32;
-    extern __shared__ __align__(16) unsigned char rsm[];
-    const RaggedSys s = sys[first + blockIdx.x];
+// Barrier of the `nthreads` threads (whole warps) of one system's group.
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// One large system on the `gwarps` warps of its group (warp index gw, named
+// barrier bar) in its shared-memory slot sized for nmax.
+template <typename T>
+__device__ __forceinline__ void large_system(const RaggedSys &s, int nmax, unsigned char *slot, int gw, int gwarps,
+                                             int bar, const T *__restrict__ A_in, T *__restrict__ A,
+                                             T *__restrict__ B, int *__restrict__ info, int refine, int lane) {
+    const int RG_LARGE_WARPS = gwarps, warp = gw, nthr = 32 * gwarps;
     const int n = s.n, nrhs = s.nrhs, ld = cta_ld(n);
     const int ldmax = cta_ld(nmax);
-    float *pbuf0 = reinterpret_cast<float *>(rsm);  // panel row r at pbuf[8 r .. 8 r + 7]
+    float *pbuf0 = reinterpret_cast<float *>(slot);  // panel row r at pbuf[8 r .. 8 r + 7]
     float *pbuf1 = pbuf0 + (size_t)nmax * 8;
     float *a = pbuf1 + (size_t)nmax * 8;
     float *dinv = a + (size_t)nmax * ldmax;
-    __shared__ int s_fail;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int *s_fail = reinterpret_cast<int *>(dinv + nmax);
     const T *ag = A_in + s.a_off;
 
     for (int j = warp; j < n; j += RG_LARGE_WARPS)
         for (int i = j + lane; i < n; i += 32) a[j * ld + i] = (float)ag[(int64_t)j * n + i];
-    if (threadIdx.x == 0) s_fail = 0;
-    __syncthreads();
+    if (gw == 0 && lane == 0) *s_fail = 0;
+    group_sync(bar, nthr);
     // Blocked right-looking factorisation with look-ahead: while warps 1..W-1
     // apply panel p's rank-8 update to the columns past panel p + 1, warp 0
     // applies it to panel p + 1's columns and factors panel p + 1 (into the
     // other panel buffer).  Each element still receives its updates in
     // increasing k with one fma each, as in the column-by-column algorithm.
     // One barrier per panel.
-    if (warp == 0) panel_factor(a, ld, n, 0, n < RG_PANEL ? n : RG_PANEL, pbuf0, dinv, &s_fail, lane);
-    __syncthreads();
+    if (warp == 0) panel_factor(a, ld, n, 0, n < RG_PANEL ? n : RG_PANEL, pbuf0, dinv, s_fail, lane);
+    group_sync(bar, nthr);
     for (int k0 = 0, p = 0; k0 < n; k0 += RG_PANEL, p++) {
         const int pw = n - k0 < RG_PANEL ? n - k0 : RG_PANEL;
         const int kn = k0 + pw, pwn = n - kn < RG_PANEL ? n - kn : RG_PANEL;  // next panel
@@ -312,14 +329,14 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
             if (pwn > 0) {
                 panel_update(a, ld, n, pb, kn, kn + pwn, 0, 1, lane);
                 __syncwarp();
-                panel_factor(a, ld, n, kn, pwn, pnext, dinv, &s_fail, lane);
+                panel_factor(a, ld, n, kn, pwn, pnext, dinv, s_fail, lane);
             }
         } else {
             panel_update(a, ld, n, pb, kn + pwn, n, warp - 1, RG_LARGE_WARPS - 1, lane);
         }
-        __syncthreads();
+        group_sync(bar, nthr);
     }
-    if (threadIdx.x == 0 && info) info[s.orig] = s_fail;
+    if (gw == 0 && lane == 0 && info) info[s.orig] = *s_fail;
 
     T *bg = B + s.b_off;
     const int nt = (n + 31) >> 5;
@@ -437,46 +454,120 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 768 / THREADS)
     }
     // L (lower triangle, FP32 factor) back in place, once every warp has
     // finished reading the original A for its residuals
-    __syncthreads();
+    group_sync(bar, nthr);
     T *aw = A + s.a_off;
     for (int j = warp; j < n; j += RG_LARGE_WARPS)
         for (int i = j + lane; i < n; i += 32) aw[(int64_t)j * n + i] = (T)a[j * ld + i];
 }
 
-// Bucket the large class (plan order: largest n first) by cfg.bucket_width:
-// bucket boundaries at 32 + w, 32 + 2w, ...; a bucket's smem is sized for its
-// first (largest) system.
-static void ragged_buckets(gbla_ragged_plan *p) {
-    p->nb = 0;
-    const int nl = p->num[3];
-    int i = 0;
-    while (i < nl && p->nb < RG_MAX_BUCKETS) {
-        const int top = p->large_n[i];
-        // bucket of top: (lo, hi] with hi - 32 a multiple of w
-        const int w = p->cfg.bucket_width;
-        const int hi = 32 + ((top - 32 + w - 1) / w) * w;
-        const int lo = (p->nb == RG_MAX_BUCKETS - 1) ? 32 : hi - w;
-        int j = i;
-        while (j < nl && p->large_n[j] > lo) j++;
-        p->b_first[p->nb] = p->first[3] + i;
-        p->b_num[p->nb] = j - i;
-        p->b_nmax[p->nb] = top;
-        p->nb++;
-        i = j;
+// ------------------------------------------------------------ persistent launch
+// Blocks pull tasks from the queue head ctr[0] until it passes ntasks; the
+// last block to finish (ctr[1]) resets both counters for the next call.  No
+// block waits on another: a block that finds the queue empty simply leaves.
+// 128 registers per thread whatever the block size (the lane-row path keeps a
+// 32-wide row and its refinement state in registers)
+template <typename T, int THREADS>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS)
+    k_ragged_persistent(const RaggedTask *__restrict__ tasks, int ntasks, const RaggedSys *__restrict__ sys,
+                        int *__restrict__ ctr, T *__restrict__ A, T *__restrict__ B, int *__restrict__ info,
+                        int refine) {
+    extern __shared__ __align__(16) unsigned char rsm[];
+    __shared__ int s_task;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (;;) {
+        if (threadIdx.x == 0) s_task = atomicAdd(ctr, 1);
+        __syncthreads();
+        const int t = s_task;
+        __syncthreads();  // every thread has read s_task before the next fetch
+        if (t >= ntasks) break;
+        const RaggedTask tk = tasks[t];
+        if (tk.nb == 0) {
+            // a launch captured before the plan's configuration changed may have
+            // less shared memory than the new task table needs: flag, never overrun
+            unsigned dyn;
+            asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+            if ((size_t)tk.count * ragged_slot_bytes(tk.nmax) > dyn) {
+                if (threadIdx.x < tk.count && info) info[sys[tk.first + threadIdx.x].orig] = -1;
+                __syncthreads();
+                continue;
+            }
+            const int grp = warp / tk.warps;  // system of the group this warp works on
+            if (grp < tk.count)
+                large_system<T>(sys[tk.first + grp], tk.nmax, rsm + (size_t)grp * ragged_slot_bytes(tk.nmax),
+                                warp % tk.warps, tk.warps, 1 + grp, A, A, B, info, refine, lane);
+        } else if (tk.nb == 8) {
+            small_systems<T, 8>(sys, tk.first, tk.count, warp, lane, A, A, B, info, refine);
+        } else if (tk.nb == 16) {
+            small_systems<T, 16>(sys, tk.first, tk.count, warp, lane, A, A, B, info, refine);
+        } else {
+            small_systems<T, 32>(sys, tk.first, tk.count, warp, lane, A, A, B, info, refine);
+        }
+        __syncthreads();  // the slots are reused by the next task
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(ctr + 1, 1) == (int)gridDim.x - 1) {
+            ctr[0] = 0;
+            ctr[1] = 0;
+            __threadfence();
+        }
     }
 }
 
+static bool config_valid(const gbla_ragged_config &c) {
+    const bool t = c.threads == 128 || c.threads == 256 || c.threads == 512;
+    const bool g = c.systems_per_block == 1 || c.systems_per_block == 2 || c.systems_per_block == 4 ||
+                   c.systems_per_block == 8;
+    return t && g && c.systems_per_block * 64 <= c.threads;  // at least two warps per system
+}
+
+constexpr size_t RG_SMEM_MAX = 226 * 1024;
+
+// Cut the plan's systems into tasks for p->cfg (host), upload them (set-up
+// time: synchronous copy) and size the block's shared memory.
+static gbla_status ragged_build_tasks(gbla_ragged_plan *p, std::vector<RaggedTask> *out = nullptr) {
+    std::vector<RaggedTask> t;
+    const int W = p->cfg.threads / 32;
+    const size_t top = p->num[3] > 0 ? ragged_slot_bytes(p->max_n_large) : 0;
+    size_t cap = top * (size_t)p->cfg.systems_per_block;
+    if (cap > RG_SMEM_MAX) cap = top > RG_SMEM_MAX ? top : (RG_SMEM_MAX / top) * top;
+    for (int i = p->first[3]; i < p->count;) {
+        const int nmax = p->large_n[i - p->first[3]];
+        const size_t slot = ragged_slot_bytes(nmax);
+        int cnt = (int)(cap / slot);
+        cnt = cnt < p->cfg.systems_per_block ? cnt : p->cfg.systems_per_block;
+        cnt = cnt < W / 2 ? cnt : W / 2;
+        cnt = cnt < p->count - i ? cnt : p->count - i;
+        if (cnt < 1) cnt = 1;
+        t.push_back({i, cnt, 0, W / cnt, nmax, 0});
+        i += cnt;
+    }
+    // small classes after the large ones, larger class first
+    const int nbs[3] = {8, 16, 32};
+    for (int c = 2; c >= 0; c--) {
+        const int per = W * (32 / nbs[c]);
+        for (int i = 0; i < p->num[c]; i += per)
+            t.push_back({p->first[c] + i, p->num[c] - i < per ? p->num[c] - i : per, nbs[c], 1, 0, 0});
+    }
+    p->ntasks = (int)t.size();
+    p->smem = cap;
+    if (out) *out = t;
+    if (t.empty()) return GBLA_SUCCESS;
+    // a set-up step: no call of the plan may still be reading the old table
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return from_cuda(e);
+    return from_cuda(cudaMemcpy(p->d_tasks, t.data(), sizeof(RaggedTask) * t.size(), cudaMemcpyHostToDevice));
+}
+
 template <typename T, int THREADS>
-static gbla_status launch_large(const gbla_ragged_plan *p, int b, T *A, T *B, int *info, int refine,
-                                cudaStream_t st) {
-    const size_t smem = ragged_large_smem<T>(p->b_nmax[b], THREADS / 32);
-    if (smem > 48 * 1024) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_ragged_large<T, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+static gbla_status launch_persistent(const gbla_ragged_plan *p, T *A, T *B, int *info, int refine, cudaStream_t st) {
+    auto kern = k_ragged_persistent<T, THREADS>;
+    if (p->smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
         if (e != cudaSuccess) return from_cuda(e);
     }
-    k_ragged_large<T, THREADS><<<p->b_num[b], THREADS, smem, st>>>(p->d_sys, p->b_first[b], p->b_nmax[b], A, A, B,
-                                                                    info, refine);
+    const int64_t grid = persistent_grid(reinterpret_cast<const void *>(kern), THREADS, p->smem, p->ntasks);
+    kern<<<(unsigned)grid, THREADS, p->smem, st>>>(p->d_tasks, p->ntasks, p->d_sys, p->d_ctr, A, B, info, refine);
     return launch_status();
 }
 
@@ -488,54 +579,9 @@ static gbla_status ragged_launch(const gbla_ragged_plan *p, T *A, T *B, int *inf
     int dev = -1;
     cudaGetDevice(&dev);
     if (dev != p->device) return GBLA_INVALID_VALUE;
-    cudaError_t e;
-    const int nsmall = p->num[0] + p->num[1] + p->num[2];
-    // streams: small classes on aux[0] when forked; large buckets alternate
-    // between the caller's stream and aux[1], aux[2]
-    const bool fork_small = p->cfg.fork_small && nsmall > 0 && p->nb > 0;
-    const int large_streams = p->nb < 3 ? p->nb : 3;
-    bool used[RG_STREAMS] = {fork_small, large_streams > 1, large_streams > 2};
-    if (used[0] || used[1] || used[2]) {
-        if ((e = cudaEventRecord(p->fork, st)) != cudaSuccess) return from_cuda(e);
-        for (int k = 0; k < RG_STREAMS; k++)
-            if (used[k] && (e = cudaStreamWaitEvent(p->aux[k], p->fork, 0)) != cudaSuccess) return from_cuda(e);
-    }
-    for (int b = 0; b < p->nb; b++) {
-        const int sidx = large_streams > 0 ? b % large_streams : 0;
-        cudaStream_t ls = sidx == 0 ? st : p->aux[sidx];
-        gbla_status s;
-        if (p->cfg.large_threads == 64) s = launch_large<T, 64>(p, b, A, B, info, refine, ls);
-        else if (p->cfg.large_threads == 128) s = launch_large<T, 128>(p, b, A, B, info, refine, ls);
-        else if (p->cfg.large_threads == 512) s = launch_large<T, 512>(p, b, A, B, info, refine, ls);
-        else s = launch_large<T, 256>(p, b, A, B, info, refine, ls);
-        if (s != GBLA_SUCCESS) return s;
-    }
-    cudaStream_t small_st = fork_small ? p->aux[0] : st;
-    const int gpw[3] = {4, 2, 1};
-    for (int c = 0; c < 3; c++) {
-        if (p->num[c] == 0) continue;
-        const unsigned grid = (unsigned)((p->num[c] + 4 * gpw[c] - 1) / (4 * gpw[c]));
-        if (c == 0)
-            k_ragged_small<T, 8><<<grid, 128, 0, small_st>>>(p->d_sys, p->first[c], p->num[c], A, A, B, info, refine);
-        else if (c == 1)
-            k_ragged_small<T, 16><<<grid, 128, 0, small_st>>>(p->d_sys, p->first[c], p->num[c], A, A, B, info, refine);
-        else
-            k_ragged_small<T, 32><<<grid, 128, 0, small_st>>>(p->d_sys, p->first[c], p->num[c], A, A, B, info, refine);
-        gbla_status s = launch_status();
-        if (s != GBLA_SUCCESS) return s;
-    }
-    for (int k = 0; k < RG_STREAMS; k++) {
-        if (!used[k]) continue;
-        if ((e = cudaEventRecord(p->join[k], p->aux[k])) != cudaSuccess) return from_cuda(e);
-        if ((e = cudaStreamWaitEvent(st, p->join[k], 0)) != cudaSuccess) return from_cuda(e);
-    }
-    return GBLA_SUCCESS;
-}
-
-static bool config_valid(const gbla_ragged_config &c) {
-    return (c.bucket_width == 16 || c.bucket_width == 32 || c.bucket_width == 48 || c.bucket_width == 96) &&
-           (c.large_threads == 64 || c.large_threads == 128 || c.large_threads == 256 || c.large_threads == 512) &&
-           (c.fork_small == 0 || c.fork_small == 1);
+    if (p->cfg.threads == 128) return launch_persistent<T, 128>(p, A, B, info, refine, st);
+    if (p->cfg.threads == 512) return launch_persistent<T, 512>(p, A, B, info, refine, st);
+    return launch_persistent<T, 256>(p, A, B, info, refine, st);
 }
 
 // Time every candidate configuration on the caller's batch.  A and B are
@@ -565,38 +611,41 @@ static gbla_status ragged_autotune(gbla_ragged_plan *p, const T *A, const T *B, 
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sa, A, abytes, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sb, B, bbytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     gbla_status status = from_cuda(e);
     const gbla_ragged_config saved = p->cfg;
     gbla_ragged_config best = saved;
     float best_t = 3.4e38f;
-    const int widths[4] = {96, 48, 32, 16}, threads[4] = {64, 128, 256, 512};
-    for (int wi = 0; wi < 4 && status == GBLA_SUCCESS; wi++)
-        for (int ti = 0; ti < 4 && status == GBLA_SUCCESS; ti++)
-            for (int f = 0; f < 2 && status == GBLA_SUCCESS; f++) {
-                p->cfg = {widths[wi], threads[ti], f};
-                ragged_buckets(p);
-                float t_min = 3.4e38f;
-                for (int r = 0; r <= reps && status == GBLA_SUCCESS; r++) {  // r = 0: warm-up
-                    e = cudaMemcpyAsync(wa, sa, abytes, cudaMemcpyDeviceToDevice, st);
-                    if (e == cudaSuccess) e = cudaMemcpyAsync(wb, sb, bbytes, cudaMemcpyDeviceToDevice, st);
-                    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
-                    if (e != cudaSuccess) { status = from_cuda(e); break; }
-                    status = ragged_launch<T>(p, wa, wb, sinfo, refine, st);
-                    if (status != GBLA_SUCCESS) break;
-                    e = cudaEventRecord(e1, st);
-                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                    float ms = 0.f;
-                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-                    if (e != cudaSuccess) { status = from_cuda(e); break; }
-                    if (r > 0 && ms < t_min) t_min = ms;
-                }
-                if (status == GBLA_SUCCESS && t_min < best_t) {
-                    best_t = t_min;
-                    best = p->cfg;
-                }
+    const int threads[3] = {128, 256, 512}, groups[4] = {1, 2, 4, 8};
+    for (int ti = 0; ti < 3 && status == GBLA_SUCCESS; ti++)
+        for (int gi = 0; gi < 4 && status == GBLA_SUCCESS; gi++) {
+            const gbla_ragged_config c = {threads[ti], groups[gi]};
+            if (!config_valid(c)) continue;
+            p->cfg = c;
+            status = ragged_build_tasks(p);
+            float t_min = 3.4e38f;
+            for (int r = 0; r <= reps && status == GBLA_SUCCESS; r++) {  // r = 0: warm-up
+                e = cudaMemcpyAsync(wa, sa, abytes, cudaMemcpyDeviceToDevice, st);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(wb, sb, bbytes, cudaMemcpyDeviceToDevice, st);
+                if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+                if (e != cudaSuccess) { status = from_cuda(e); break; }
+                status = ragged_launch<T>(p, wa, wb, sinfo, refine, st);
+                if (status != GBLA_SUCCESS) break;
+                e = cudaEventRecord(e1, st);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e != cudaSuccess) { status = from_cuda(e); break; }
+                if (r > 0 && ms < t_min) t_min = ms;
             }
+            if (status == GBLA_SUCCESS && t_min < best_t) {
+                best_t = t_min;
+                best = c;
+            }
+        }
     p->cfg = status == GBLA_SUCCESS ? best : saved;
-    ragged_buckets(p);
+    gbla_status s2 = ragged_build_tasks(p);
+    if (status == GBLA_SUCCESS) status = s2;
     cudaStreamSynchronize(st);
     if (sa) cudaFree(sa);
     if (sb) cudaFree(sb);
@@ -646,19 +695,19 @@ GBLA_API gbla_status gbla_ragged_plan_create(const int64_t *a_offsets, const int
     for (int c = 1; c < 4; c++) p->first[c] = p->first[c - 1] + p->num[c - 1];
     p->max_n_large = p->num[3] > 0 ? v[p->first[3]].n : 0;
     for (int i = p->first[3]; i < count; i++) p->large_n.push_back(v[i].n);
-    ragged_buckets(p);
     cudaError_t e = cudaGetDevice(&p->device);
     if (e == cudaSuccess && count > 0) e = cudaMalloc(&p->d_sys, sizeof(RaggedSys) * (size_t)count);
     if (e == cudaSuccess && count > 0)
         e = cudaMemcpy(p->d_sys, v.data(), sizeof(RaggedSys) * (size_t)count, cudaMemcpyHostToDevice);
-    for (int k = 0; k < RG_STREAMS && e == cudaSuccess; k++) {
-        e = cudaStreamCreateWithFlags(&p->aux[k], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->join[k], cudaEventDisableTiming);
-    }
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
-    if (e != cudaSuccess) {
+    // at most one task per system
+    if (e == cudaSuccess && count > 0) e = cudaMalloc(&p->d_tasks, sizeof(RaggedTask) * (size_t)count);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_ctr, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->d_ctr, 0, 2 * sizeof(int));
+    gbla_status s = from_cuda(e);
+    if (s == GBLA_SUCCESS && count > 0) s = ragged_build_tasks(p);
+    if (s != GBLA_SUCCESS) {
         gbla_ragged_plan_destroy(p);
-        return from_cuda(e);
+        return s;
     }
     *plan = p;
     return GBLA_SUCCESS;
@@ -667,17 +716,15 @@ GBLA_API gbla_status gbla_ragged_plan_create(const int64_t *a_offsets, const int
 GBLA_API gbla_status gbla_ragged_plan_destroy(gbla_ragged_plan *p) {
     if (!p) return GBLA_SUCCESS;
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < RG_STREAMS; k++)
-        if (p->aux[k]) {
-            cudaError_t e2 = cudaStreamSynchronize(p->aux[k]);
-            if (e == cudaSuccess) e = e2;
-        }
-    if (p->d_sys) cudaFree(p->d_sys);
-    for (int k = 0; k < RG_STREAMS; k++) {
-        if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
-        if (p->join[k]) cudaEventDestroy(p->join[k]);
+    if (p->d_sys) e = cudaFree(p->d_sys);
+    if (p->d_tasks) {
+        cudaError_t e2 = cudaFree(p->d_tasks);
+        if (e == cudaSuccess) e = e2;
     }
-    if (p->fork) cudaEventDestroy(p->fork);
+    if (p->d_ctr) {
+        cudaError_t e2 = cudaFree(p->d_ctr);
+        if (e == cudaSuccess) e = e2;
+    }
     delete p;
     return from_cuda(e);
 }
@@ -691,7 +738,13 @@ GBLA_API gbla_status gbla_ragged_plan_get_config(const gbla_ragged_plan *p, gbla
 GBLA_API gbla_status gbla_ragged_plan_set_config(gbla_ragged_plan *p, const gbla_ragged_config *cfg) {
     if (!p || !cfg || !config_valid(*cfg)) return GBLA_INVALID_VALUE;
     p->cfg = *cfg;
-    ragged_buckets(p);
+    return p->count > 0 ? ragged_build_tasks(p) : GBLA_SUCCESS;
+}
+
+GBLA_API gbla_status gbla_ragged_plan_tasks(const gbla_ragged_plan *p, int *ntasks, size_t *smem_bytes) {
+    if (!p) return GBLA_INVALID_VALUE;
+    if (ntasks) *ntasks = p->ntasks;
+    if (smem_bytes) *smem_bytes = p->smem;
     return GBLA_SUCCESS;
 }
 

@@ -78,7 +78,11 @@ gbla_status gbla_dgemm_batched(int m, int n, int k, double alpha, const double *
  * upper triangle is not touched.  info[i] = 0 on success, j if the leading
  * minor of order j is not positive definite.
  * Replaces cusolverDn<t>potrfBatched (include/tensor.cuh:2135-2159) and
- * cusolverDn<t>potrf (include/tensor.cuh:1742-1761).  n <= 128. */
+ * cusolverDn<t>potrf (include/tensor.cuh:1742-1761).  Any n: n <= 32 one
+ * group of lanes per matrix in registers; larger n one block per matrix, the
+ * matrix in shared memory when it fits (n up to ~230 float / ~160 double),
+ * else factored in place in A (n up to ~6400 float / ~3200 double, where the
+ * block's solve columns still fit in shared memory). */
 gbla_status gbla_spotrf_batched(int n, float *A, int64_t strideA, int *info, int batch,
                                 cudaStream_t stream);
 gbla_status gbla_dpotrf_batched(int n, double *A, int64_t strideA, int *info, int batch,
@@ -87,7 +91,7 @@ gbla_status gbla_dpotrf_batched(int n, double *A, int64_t strideA, int *info, in
 /* Solve L_i L_i^T X_i = B_i in place (B_i is n x nrhs) with the lower factor
  * in L_i.  Replaces cusolverDn<t>potrsBatched (include/tensor.cuh:2161-2197)
  * and cusolverDn<t>potrs (include/tensor.cuh:1763-1783); nrhs >= 1 (the
- * reference supports nrhs = 1 only).  n <= 128. */
+ * reference supports nrhs = 1 only).  Sizes as gbla_spotrf_batched. */
 gbla_status gbla_spotrs_batched(int n, int nrhs, const float *L, int64_t strideL, float *B,
                                 int64_t strideB, int batch, cudaStream_t stream);
 gbla_status gbla_dpotrs_batched(int n, int nrhs, const double *L, int64_t strideL, double *B,
@@ -97,7 +101,10 @@ gbla_status gbla_dpotrs_batched(int n, int nrhs, const double *L, int64_t stride
  * A_i and X_i in B_i.  refine_iters refinement steps use an extended-
  * precision residual B_i - A_i X_i computed from the original A_i.  Equivalent
  * to CholeskyBatchFactoriser::factorise() followed by solve()
- * (include/tensor.cuh:2135-2197) for any nrhs.  n <= 128. */
+ * (include/tensor.cuh:2135-2197) for any nrhs.  Sizes as gbla_spotrf_batched;
+ * refinement needs the matrix in shared memory (n up to ~230 float / ~160
+ * double: the original stays in A meanwhile) and returns GBLA_NOT_SUPPORTED
+ * beyond it (refine_iters = 0 works for every size). */
 gbla_status gbla_sposv_batched(int n, int nrhs, float *A, int64_t strideA, float *B,
                                int64_t strideB, int *info, int refine_iters, int batch,
                                cudaStream_t stream);
@@ -108,44 +115,54 @@ gbla_status gbla_dposv_batched(int n, int nrhs, double *A, int64_t strideA, doub
 /* Ragged batches: SPD systems of mixed size in one call.  System i has its
  * n_i x n_i matrix at A + a_offsets[i] and its n_i x nrhs_i right-hand sides
  * at B + b_offsets[i] (element offsets, column-major, 1 <= n_i <= 128).
- * The plan sorts the systems into size classes (largest first) once; it owns
- * a small device table, three auxiliary streams and four events, so create it
- * at set-up time (it allocates and synchronises) and do not use one plan from
- * two host threads at once.  No reference counterpart: GPUtils needs one
- * CholeskyBatchFactoriser per size and one potrs per column
- * (include/tensor.cuh:2100-2197). */
+ * The plan sorts the systems (size class, then largest first) and cuts them
+ * into tasks once; a call is then ONE persistent kernel launch whose blocks
+ * take tasks from a device queue.  The plan owns small device tables and the
+ * queue counter, so create it at set-up time (it allocates and synchronises),
+ * and do not run calls of one plan concurrently (two host threads, or two
+ * streams whose calls overlap on the GPU): they share the queue.  No
+ * reference counterpart: GPUtils needs one CholeskyBatchFactoriser per size
+ * and one potrs per column (include/tensor.cuh:2100-2197). */
 typedef struct gbla_ragged_plan gbla_ragged_plan;
 gbla_status gbla_ragged_plan_create(const int64_t *a_offsets, const int64_t *b_offsets, const int *n,
                                     const int *nrhs, int count, gbla_ragged_plan **plan);
 gbla_status gbla_ragged_plan_destroy(gbla_ragged_plan *plan);
 
-/* Launch configuration of a plan.  Systems with n <= 32 run the lane-row
- * kernel (8, 16 or 32 lanes per system); the n > 32 systems run one block per
- * system, cut into buckets of width bucket_width in n (96: one bucket; 48, 32,
- * 16: more launches, each sized for its own largest system), with
- * large_threads threads per block (64, 128, 256, 512); fork_small puts the small
- * classes on their own forked stream.  Default {96, 256, 1}.  The result of a
- * call does not depend on the configuration (bit-identical). */
+/* Launch configuration of a plan: threads per block (128, 256, 512) and the
+ * most systems with n > 32 that one block factors at once (1, 2, 4, 8; at
+ * most threads / 64), each with threads / 32 / count warps and its own
+ * shared-memory slot (sized for the group's largest system; the block's
+ * shared memory -- and so the blocks per SM -- is that many slots of the
+ * plan's largest system).  Systems with n <= 32 run the lane-row method,
+ * 32 / NB systems per warp.  Default {256, 2}.  Set-up calls: set_config
+ * waits for the device and uploads the new task table, so a CUDA graph
+ * captured before it must be captured again (its launch keeps the old grid
+ * and shared-memory size; a task that no longer fits is skipped and reports
+ * info = -1 for its systems).  The result of a call does not depend on the
+ * configuration (bit-identical). */
 typedef struct gbla_ragged_config {
-    int bucket_width;
-    int large_threads;
-    int fork_small;
+    int threads;
+    int systems_per_block;
 } gbla_ragged_config;
 gbla_status gbla_ragged_plan_get_config(const gbla_ragged_plan *plan, gbla_ragged_config *config);
 gbla_status gbla_ragged_plan_set_config(gbla_ragged_plan *plan, const gbla_ragged_config *config);
+/* Tasks of the current configuration and the dynamic shared memory of a block
+ * (either pointer nullable). */
+gbla_status gbla_ragged_plan_tasks(const gbla_ragged_plan *plan, int *ntasks, size_t *smem_bytes);
 
-/* Autotuner: times every configuration (4 bucket widths x 4 block sizes x 2
- * stream layouts) on this batch -- best of `reps` runs after a warm-up, each
- * on fresh copies of A and B -- and keeps the fastest in the plan.  A and B
- * are not modified.  best / best_ms (nullable) receive the choice and its
- * time.  Allocates scratch copies and synchronises: a set-up call. */
+/* Autotuner: times every valid configuration (threads x systems per block,
+ * 9 candidates) on this batch -- best of `reps` runs after a warm-up, each on
+ * fresh copies of A and B -- and keeps the fastest in the plan.  A and B are
+ * not modified.  best / best_ms (nullable) receive the choice and its time.
+ * Allocates scratch copies and synchronises: a set-up call. */
 gbla_status gbla_sragged_autotune(gbla_ragged_plan *plan, const float *A, const float *B, int refine_iters,
                                   int reps, gbla_ragged_config *best, float *best_ms, cudaStream_t stream);
 gbla_status gbla_dragged_autotune(gbla_ragged_plan *plan, const double *A, const double *B, int refine_iters,
                                   int reps, gbla_ragged_config *best, float *best_ms, cudaStream_t stream);
 
 /* Factor + solve every system of the plan (device on which the plan was
- * created; stream-ordered; graph-capturable).  A_i receives its FP32 Cholesky
+ * created; one kernel launch, stream-ordered, graph-capturable: the queue
+ * counter is reset by the launch itself).  A_i receives its FP32 Cholesky
  * factor (lower triangle), B_i the solutions, info[i] the potrf status.  The
  * factorisation runs in FP32; refine_iters refinement steps recompute
  * B - A X from the full symmetric original A_i (both triangles must be
@@ -388,6 +405,30 @@ gbla_status gbla_drot_dev(int64_t len, double *x, int64_t incx, double *y, int64
 gbla_status gbla_sgivens_coeffs(const float *A, int64_t ld, int i, int k, int j, float *out, cudaStream_t stream);
 gbla_status gbla_dgivens_coeffs(const double *A, int64_t ld, int i, int k, int j, double *out,
                                 cudaStream_t stream);
+
+/* Batched forms of the two Givens calls above.  GPUtils applies a rotation
+ * to one matrix at a time (applyLeft/RightGivensRotation and
+ * GivensAnnihilator throw for tensors with numMats > 1, include/tensor.cuh:
+ * 1074-1104, 2200-2312); these rotate every matrix of a batch in one launch.
+ * rot_batched: problem b rotates x + b stride and y + b stride (len entries,
+ * increments incx, incy) with c = c[b cs_stride], s = s[b cs_stride] (device
+ * memory): x <- c x + s y, y <- c y - s x.  The left rotation of rows i, k of
+ * every m x n matrix is x = A + i, y = A + k, incx = incy = m, stride = m n;
+ * the right rotation of columns i, k is x = A + i m, y = A + k m, inc 1. */
+gbla_status gbla_srot_batched(int64_t len, float *x, int64_t incx, float *y, int64_t incy, int64_t stride,
+                              const float *c, const float *s, int64_t cs_stride, int batch, cudaStream_t stream);
+gbla_status gbla_drot_batched(int64_t len, double *x, int64_t incx, double *y, int64_t incy, int64_t stride,
+                              const double *c, const double *s, int64_t cs_stride, int batch, cudaStream_t stream);
+/* GivensAnnihilator::annihilate(i, k, j) on every m x n matrix of a batch:
+ * each matrix gets its own rotation of rows i and k that zeroes its (k, j)
+ * entry (r = 1 / hypot(A(i,j), A(k,j)), c = A(i,j) r, s = A(k,j) r, as
+ * k_givensAnnihilateRHypot + cublas<t>rot, include/tensor.cuh:2270-2311).
+ * coeffs (nullable) receives (r, c, s) per matrix (3 batch entries).
+ * i != k, i, k < m, j < n (invalid value otherwise). */
+gbla_status gbla_sgivens_annihilate_batched(int m, int n, float *A, int64_t strideA, int i, int k, int j,
+                                            float *coeffs, int batch, cudaStream_t stream);
+gbla_status gbla_dgivens_annihilate_batched(int m, int n, double *A, int64_t strideA, int i, int k, int j,
+                                            double *coeffs, int batch, cudaStream_t stream);
 
 /* ------------------------------------------ BF16 tensor-core GEMM (TN) */
 /* Fused epilogue of gbla_gemm_bf16_tn, applied per element in this order:

@@ -20,9 +20,14 @@
  *    right-hand-side columns (the reference throws or solves only one).
  *  - leastSquaresBatched (float) adds one refinement step with an extended-
  *    precision residual, so x is accurate to FP32 rounding even when the
- *    residual is large (cuBLAS gelsBatched: about kappa^2 u).
+ *    residual is large (cuBLAS gelsBatched: about kappa^2 u); matrices too
+ *    large for a shared-memory working copy (m n above ~50k) are solved
+ *    without it, like cuBLAS.
  *  - operator= releases what the target owned before aliasing the source.
  *  - Givens bounds are checked on every index, as the reference documents.
+ *  - Extensions with no reference counterpart: batched Givens rotations
+ *    (DTensor::applyLeft/RightGivensRotationBatched, GivensAnnihilatorBatched),
+ *    which rotate every matrix of a tensor in one launch.
  */
 #ifndef TENSOR_CUH
 #define TENSOR_CUH
@@ -241,6 +246,22 @@ inline gbla_status rot_dev(int64_t n, double *x, int64_t ix, double *y, int64_t 
                            cudaStream_t st) {
     return gbla_drot_dev(n, x, ix, y, iy, c, s, st);
 }
+inline gbla_status rot_batched(int64_t n, float *x, int64_t ix, float *y, int64_t iy, int64_t stride, const float *c,
+                               const float *s, int batch, cudaStream_t st) {
+    return gbla_srot_batched(n, x, ix, y, iy, stride, c, s, 1, batch, st);
+}
+inline gbla_status rot_batched(int64_t n, double *x, int64_t ix, double *y, int64_t iy, int64_t stride,
+                               const double *c, const double *s, int batch, cudaStream_t st) {
+    return gbla_drot_batched(n, x, ix, y, iy, stride, c, s, 1, batch, st);
+}
+inline gbla_status annihilate_batched(int m, int n, float *A, int i, int k, int j, float *co, int batch,
+                                      cudaStream_t st) {
+    return gbla_sgivens_annihilate_batched(m, n, A, (int64_t)m * n, i, k, j, co, batch, st);
+}
+inline gbla_status annihilate_batched(int m, int n, double *A, int i, int k, int j, double *co, int batch,
+                                      cudaStream_t st) {
+    return gbla_dgivens_annihilate_batched(m, n, A, (int64_t)m * n, i, k, j, co, batch, st);
+}
 inline gbla_status givens(const float *A, int64_t ld, int i, int k, int j, float *o, cudaStream_t st) {
     return gbla_sgivens_coeffs(A, ld, i, k, j, o, st);
 }
@@ -260,7 +281,12 @@ inline gbla_status potrs(int n, int nrhs, const double *L, double *B, int batch,
     return gbla_dpotrs_batched(n, nrhs, L, (int64_t)n * n, B, (int64_t)n * nrhs, batch, st);
 }
 inline gbla_status gels(int m, int n, int nrhs, float *A, float *B, int batch, cudaStream_t st) {
-    return gbla_sgels_batched(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, 1, batch, st);
+    gbla_status s = gbla_sgels_batched(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, 1, batch, st);
+    // refinement needs a shared-memory working copy of A; beyond that (checked
+    // before anything runs) solve without it, as cuBLAS does
+    if (s == GBLA_NOT_SUPPORTED)
+        s = gbla_sgels_batched(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, 0, batch, st);
+    return s;
 }
 inline gbla_status gels(int m, int n, int nrhs, double *A, double *B, int batch, cudaStream_t st) {
     return gbla_dgels_batched(m, n, nrhs, A, (int64_t)m * n, B, (int64_t)m * nrhs, nullptr, batch, st);
@@ -603,6 +629,33 @@ public:
         gputils_detail::check(gputils_detail::rot_dev((int64_t)m_numCols, m_d_data + i, (int64_t)m_numRows,
                                                       m_d_data + j, (int64_t)m_numRows, d_c, d_minus_s, st()),
                               "applyLeftGivensRotation");
+    }
+
+    /** Extension (the reference rotates one matrix at a time): left rotation
+     * of rows i and j of every matrix, matrix b with c(0,0,b) and
+     * minus_s(0,0,b) from device tensors of shape (1, 1, numMats). */
+    void applyLeftGivensRotationBatched(size_t i, size_t j, const DTensor<T> &c, const DTensor<T> &minus_s) {
+        if (i >= m_numRows || j >= m_numRows) throw std::invalid_argument("[applyLeftGivensRotation] invalid index");
+        if (c.numEl() != m_numMats || minus_s.numEl() != m_numMats)
+            throw std::invalid_argument("[applyLeftGivensRotationBatched] one (c, s) per matrix");
+        gputils_detail::check(gputils_detail::rot_batched((int64_t)m_numCols, m_d_data + i, (int64_t)m_numRows,
+                                                          m_d_data + j, (int64_t)m_numRows,
+                                                          (int64_t)(m_numRows * m_numCols), c.raw(), minus_s.raw(),
+                                                          (int)m_numMats, st()),
+                              "applyLeftGivensRotationBatched");
+    }
+
+    /** Extension: right rotation of columns i and j of every matrix, with
+     * per-matrix (c, -s) as applyLeftGivensRotationBatched. */
+    void applyRightGivensRotationBatched(size_t i, size_t j, const DTensor<T> &c, const DTensor<T> &minus_s) {
+        if (i >= m_numCols || j >= m_numCols) throw std::invalid_argument("[applyRightGivensRotation] invalid index");
+        if (c.numEl() != m_numMats || minus_s.numEl() != m_numMats)
+            throw std::invalid_argument("[applyRightGivensRotationBatched] one (c, s) per matrix");
+        gputils_detail::check(gputils_detail::rot_batched((int64_t)m_numRows, m_d_data + i * m_numRows, 1,
+                                                          m_d_data + j * m_numRows, 1,
+                                                          (int64_t)(m_numRows * m_numCols), c.raw(), minus_s.raw(),
+                                                          (int)m_numMats, st()),
+                              "applyRightGivensRotationBatched");
     }
 
     void leastSquaresBatched(DTensor &B) {
@@ -1071,6 +1124,39 @@ public:
                               "GivensAnnihilator");
         m_matrix->applyLeftGivensRotationDevice(i, k, aux + 1, aux + 2);
     }
+};
+
+/* ------------------------------------------------ GivensAnnihilatorBatched */
+/** Extension: GivensAnnihilator for a tensor of any number of matrices --
+ * annihilate(i, k, j) zeroes element (k, j) of every matrix, each with its
+ * own rotation of rows i and k, in one launch.  coefficients() holds
+ * (1 / hypot, cos, sin) per matrix, shape (3, 1, numMats). */
+TEMPLATE_WITH_TYPE_T
+TEMPLATE_CONSTRAINT_REQUIRES_FPX
+class GivensAnnihilatorBatched {
+private:
+    DTensor<T> *m_matrix = nullptr;
+    std::unique_ptr<DTensor<T>> m_coeffs;
+
+public:
+    GivensAnnihilatorBatched(DTensor<T> &a) { setMatrix(a); }
+
+    void setMatrix(DTensor<T> &a) {
+        m_matrix = &a;
+        if (!m_coeffs || m_coeffs->numMats() != a.numMats()) m_coeffs = std::make_unique<DTensor<T>>(3, 1, a.numMats());
+    }
+
+    void annihilate(size_t i, size_t k, size_t j) {
+        size_t nR = m_matrix->numRows(), nC = m_matrix->numCols();
+        if (i >= nR || k >= nR || i == k) throw std::invalid_argument("[GivensAnnihilatorBatched] invalid row index");
+        if (j >= nC) throw std::invalid_argument("[GivensAnnihilatorBatched] invalid column index j");
+        cudaStream_t st = Session::getInstance().stream(m_matrix->streamIdx());
+        gputils_detail::check(gputils_detail::annihilate_batched((int)nR, (int)nC, m_matrix->raw(), (int)i, (int)k,
+                                                                 (int)j, m_coeffs->raw(), (int)m_matrix->numMats(), st),
+                              "GivensAnnihilatorBatched");
+    }
+
+    DTensor<T> const &coefficients() const { return *m_coeffs; }
 };
 
 #endif  // TENSOR_CUH

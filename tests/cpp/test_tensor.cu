@@ -4,6 +4,7 @@
 // int).  Golden values come from goldens.h (read from the reference's tests).
 // Prints one line per test and exits non-zero if any check failed.
 #include <cstdio>
+#include <random>
 #include <functional>
 #include <numeric>
 #include <string>
@@ -554,6 +555,187 @@ TEST(givensAnnihilateCorrectness) {
     EXPECT_NEAR(golden::givens_a03, a(0, 3), 1e-12);
     EXPECT_NEAR(golden::givens_a13, a(1, 3), 1e-12);
 }
+
+// ------------------------------------- shapes beyond the warp kernels (extensions of coverage)
+template <typename T> static std::vector<T> randomVec(size_t len, unsigned seed) {
+    std::mt19937 gen(seed);
+    std::normal_distribution<double> d(0.0, 1.0);
+    std::vector<T> v(len);
+    for (auto &x : v) x = (T)d(gen);
+    return v;
+}
+
+// leastSquaresBatched on 128 x 64 (and 100 x 50): the normal equations hold
+template <typename T> static void lsBig(size_t m, size_t n, T eps) {
+    const size_t k = 3;
+    std::vector<T> a = randomVec<T>(m * n * k, 11), b = randomVec<T>(m * k, 12);
+    DTensor<T> A(a, m, n, k), B(b, m, 1, k), A0(a, m, n, k), B0(b, m, 1, k);
+    A.leastSquaresBatched(B);
+    std::vector<T> x;
+    B.download(x);
+    for (size_t i = 0; i < k; i++) {
+        // A^T (b - A x) = 0 relative to |A| |b|
+        double worst = 0, na = 0, nb = 0;
+        for (size_t e = 0; e < m * n; e++) na += (double)a[i * m * n + e] * a[i * m * n + e];
+        for (size_t r = 0; r < m; r++) nb += (double)b[i * m + r] * b[i * m + r];
+        std::vector<double> res(m);
+        for (size_t r = 0; r < m; r++) {
+            double acc = b[i * m + r];
+            for (size_t c = 0; c < n; c++) acc -= (double)a[i * m * n + c * m + r] * x[i * m + c];
+            res[r] = acc;
+        }
+        for (size_t c = 0; c < n; c++) {
+            double g = 0;
+            for (size_t r = 0; r < m; r++) g += (double)a[i * m * n + c * m + r] * res[r];
+            worst = std::max(worst, std::abs(g));
+        }
+        EXPECT_LT(worst / std::sqrt(na * nb), eps);
+    }
+}
+TEST(leastSquaresBatchedBeyond128x32) {
+    lsBig<float>(128, 64, 1e-5f); lsBig<double>(128, 64, 1e-12);
+    lsBig<float>(100, 50, 1e-5f); lsBig<double>(256, 100, 1e-12);
+}
+
+// QRFactoriser on 100 x 50: Q R == A, Q^T Q == I, least squares as above
+template <typename T> static void qrBig(size_t m, size_t n, T eps) {
+    std::vector<T> a = randomVec<T>(m * n, 21);
+    DTensor<T> A(a, m, n), work(a, m, n);
+    QRFactoriser<T> qr(work);
+    qr.factorise();
+    EXPECT_EQ(0, qr.info()(0));
+    DTensor<T> Q(m, n), R(n, n);
+    qr.getQR(Q, R);
+    DTensor<T> QR_(m, n);
+    QR_.addAB(Q, R);
+    QR_ -= A;
+    EXPECT_LT(QR_.normF() / A.normF(), eps);
+    DTensor<T> QtQ(n, n);
+    DTensor<T> Qt = Q.tr();
+    QtQ.addAB(Qt, Q);
+    std::vector<T> q;
+    QtQ.download(q);
+    double worst = 0;
+    for (size_t c = 0; c < n; c++)
+        for (size_t r = 0; r < n; r++) worst = std::max(worst, std::abs((double)q[c * n + r] - (r == c ? 1.0 : 0.0)));
+    EXPECT_LT(worst, eps * 10);
+}
+TEST(qrFactoriserBeyond128x32) { qrBig<float>(100, 50, 1e-5f); qrBig<double>(256, 100, 1e-12); qrBig<double>(128, 128, 1e-12); }
+
+// Svd with U on 96 x 96 and 200 x 128: A == U S V^T, S descending
+template <typename T> static void svdBig(size_t m, size_t n, T eps) {
+    std::vector<T> a = randomVec<T>(m * n, 31);
+    DTensor<T> A(a, m, n);
+    Svd<T> svd(A, true, false);
+    svd.factorise();
+    EXPECT_EQ(0, svd.info()(0));
+    std::vector<T> S, Vt, U;
+    svd.singularValues().download(S);
+    svd.rightSingularVectors().download(Vt);
+    (*svd.leftSingularVectors().value()).download(U);
+    for (size_t j = 1; j < n; j++) EXPECT_TRUE(S[j] <= S[j - 1]);
+    double num = 0, den = 0;
+    for (size_t c = 0; c < n; c++)
+        for (size_t r = 0; r < m; r++) {
+            double acc = 0;
+            for (size_t l = 0; l < n; l++) acc += (double)U[l * m + r] * S[l] * Vt[c * n + l];
+            num += (acc - a[c * m + r]) * (acc - a[c * m + r]);
+            den += (double)a[c * m + r] * a[c * m + r];
+        }
+    EXPECT_LT(std::sqrt(num / den), eps);
+}
+TEST(svdBeyond64Columns) { svdBig<float>(96, 96, 1e-5f); svdBig<float>(200, 128, 1e-5f); svdBig<double>(128, 128, 1e-12); }
+
+// Nullspace of 100 x 140: A N == 0, N^T N == I on the kernel columns
+template <typename T> static void nullspaceBig(size_t m, size_t n, T eps) {
+    std::vector<T> a = randomVec<T>(m * n, 41);
+    DTensor<T> A(a, m, n);
+    Nullspace<T> ns(A);
+    DTensor<T> N = ns.nullspace();
+    DTensor<T> AN(m, n);
+    AN.addAB(A, N);
+    EXPECT_LT(AN.normF(), eps * A.normF());
+    DTensor<T> Nt = N.tr();
+    DTensor<T> NtN(n, n);
+    NtN.addAB(Nt, N);
+    std::vector<T> g;
+    NtN.download(g);
+    double tr = 0;
+    for (size_t i = 0; i < n; i++) tr += g[i * n + i];
+    EXPECT_NEAR(tr, (double)(n - m), 1e-3);
+}
+TEST(nullspaceBeyond64Rows) { nullspaceBig<float>(100, 140, 1e-4f); nullspaceBig<double>(120, 130, 1e-10); }
+
+// CholeskyBatchFactoriser for n = 200 (shared memory, float) and 300 (global memory, double)
+template <typename T> static void choleskyBig(size_t n, T eps) {
+    const size_t k = 2;
+    std::vector<T> g = randomVec<T>(n * n * k, 51), a(n * n * k, T(0));
+    for (size_t i = 0; i < k; i++)
+        for (size_t c = 0; c < n; c++)
+            for (size_t r = 0; r < n; r++) {
+                double acc = r == c ? 0.5 : 0.0;
+                for (size_t l = 0; l < n; l++) acc += (double)g[i * n * n + r * n + l] * g[i * n * n + c * n + l] / n;
+                a[i * n * n + c * n + r] = (T)acc;
+            }
+    DTensor<T> A(a, n, n, k), b(randomVec<T>(n * k, 52), n, 1, k), b0 = b;
+    CholeskyBatchFactoriser<T> chol(A);
+    chol.factorise();
+    chol.solve(b);
+    std::vector<T> x, bb;
+    b.download(x);
+    b0.download(bb);
+    for (size_t i = 0; i < k; i++) {
+        double num = 0, den = 0;
+        for (size_t r = 0; r < n; r++) {
+            double acc = 0;
+            for (size_t c = 0; c < n; c++) acc += (double)a[i * n * n + c * n + r] * x[i * n + c];
+            num += (acc - bb[i * n + r]) * (acc - bb[i * n + r]);
+            den += (double)bb[i * n + r] * bb[i * n + r];
+        }
+        EXPECT_LT(std::sqrt(num / den), eps);
+    }
+}
+TEST(choleskyBatchBeyond128) { choleskyBig<float>(200, 1e-4f); choleskyBig<double>(300, 1e-11); }
+
+// GivensAnnihilatorBatched zeroes (k, j) of every matrix with its own rotation;
+// applyLeftGivensRotationBatched with those coefficients reproduces it
+template <typename T> static void givensBatched(T eps) {
+    const size_t m = 5, n = 7, k = 9;
+    std::vector<T> a = randomVec<T>(m * n * k, 61);
+    DTensor<T> A(a, m, n, k), B(a, m, n, k);
+    GivensAnnihilatorBatched<T> ga(A);
+    ga.annihilate(1, 3, 2);
+    std::vector<T> got;
+    A.download(got);
+    for (size_t i = 0; i < k; i++) EXPECT_LT(std::abs((double)got[i * m * n + 2 * m + 3]), eps);
+    std::vector<T> co;
+    ga.coefficients().download(co);
+    std::vector<T> cv(k), sv(k);
+    for (size_t i = 0; i < k; i++) { cv[i] = co[3 * i + 1]; sv[i] = co[3 * i + 2]; }
+    DTensor<T> c(cv, 1, 1, k), s(sv, 1, 1, k);
+    B.applyLeftGivensRotationBatched(1, 3, c, s);
+    std::vector<T> got2;
+    B.download(got2);
+    double worst = 0;
+    for (size_t e = 0; e < got.size(); e++) worst = std::max(worst, std::abs((double)got[e] - got2[e]));
+    EXPECT_LT(worst, eps);
+    EXPECT_THROW(ga.annihilate(2, 2, 0), std::invalid_argument);
+    // right rotation of columns 0 and 4 of every matrix; column norms are preserved
+    DTensor<T> C(a, m, n, k);
+    C.applyRightGivensRotationBatched(0, 4, c, s);
+    std::vector<T> got3;
+    C.download(got3);
+    for (size_t i = 0; i < k; i++) {
+        double before = 0, after = 0;
+        for (size_t r = 0; r < m; r++) {
+            before += (double)a[i * m * n + r] * a[i * m * n + r] + (double)a[i * m * n + 4 * m + r] * a[i * m * n + 4 * m + r];
+            after += (double)got3[i * m * n + r] * got3[i * m * n + r] +
+                     (double)got3[i * m * n + 4 * m + r] * got3[i * m * n + 4 * m + r];
+        }
+        EXPECT_NEAR(before, after, eps * 100);
+    }
+}
+TEST(givensBatchedExtension) { givensBatched<float>(PRECISION_LOW); givensBatched<double>(PRECISION_HIGH); }
 
 int main(int argc, char **argv) {
     int failed_tests = 0;

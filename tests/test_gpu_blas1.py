@@ -156,3 +156,67 @@ def test_copy_rows_golden(gbla_lib, cuda, dt):
     assert getattr(gbla_lib, f"gbla_{p}copy_rows")(3, 3, 1, 2, ptr(Ad) + 9 * Ad.element_size(), ptr(out),
                                                     stream()) == 0
     assert np.array_equal(out.cpu().numpy(), np.array(G["getRows_expected1"], dtype=dt))
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_givens_annihilate_batched(gbla_lib, cuda, dt):
+    """Every matrix gets its own rotation of rows i, k zeroing (k, j): the
+    batched form of GivensAnnihilator::annihilate, checked against a numpy
+    restatement of k_givensAnnihilateRHypot + rot on each matrix."""
+    import torch
+    rng = np.random.default_rng(11)
+    k, m, n = 37, 6, 9
+    A = rng.standard_normal((k, m, n))
+    Ad = to_dev(A, dt)
+    co = torch.zeros(3 * k, dtype=Ad.dtype, device="cuda")
+    p = PFX[dt]
+    assert getattr(gbla_lib, f"gbla_{p}givens_annihilate_batched")(m, n, ptr(Ad), m * n, 4, 1, 3, ptr(co), k,
+                                                                    stream()) == 0
+    got = from_dev(Ad, k, m, n)
+    want = A.copy()
+    r = 1.0 / np.hypot(A[:, 4, 3], A[:, 1, 3])
+    c, s = A[:, 4, 3] * r, A[:, 1, 3] * r
+    want[:, 4, :] = c[:, None] * A[:, 4, :] + s[:, None] * A[:, 1, :]
+    want[:, 1, :] = c[:, None] * A[:, 1, :] - s[:, None] * A[:, 4, :]
+    tol = 1e-5 if dt == np.float32 else 1e-13
+    assert np.abs(got - want).max() < tol
+    assert np.abs(got[:, 1, 3]).max() < tol
+    np.testing.assert_allclose(co.cpu().numpy().reshape(k, 3), np.stack([r, c, s], 1), rtol=tol)
+    # invalid: i == k, out-of-range row
+    assert getattr(gbla_lib, f"gbla_{p}givens_annihilate_batched")(m, n, ptr(Ad), m * n, 2, 2, 0, None, k,
+                                                                    stream()) == 1
+    assert getattr(gbla_lib, f"gbla_{p}givens_annihilate_batched")(m, n, ptr(Ad), m * n, 6, 1, 0, None, k,
+                                                                    stream()) == 1
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_rot_batched_left_and_right(gbla_lib, cuda, dt):
+    import torch
+    rng = np.random.default_rng(12)
+    k, m, n = 50, 8, 5
+    A = rng.standard_normal((k, m, n))
+    th = rng.uniform(0, 2 * np.pi, k)
+    c, s = np.cos(th), np.sin(th)
+    cd = torch.tensor(c, dtype=torch.float32 if dt == np.float32 else torch.float64, device="cuda")
+    sd = torch.tensor(s, dtype=cd.dtype, device="cuda")
+    p = PFX[dt]
+    tol = 1e-5 if dt == np.float32 else 1e-13
+    # left: rows 2 and 6 of every matrix
+    Ad = to_dev(A, dt)
+    base = ptr(Ad)
+    es = Ad.element_size()
+    assert getattr(gbla_lib, f"gbla_{p}rot_batched")(n, base + 2 * es, m, base + 6 * es, m, m * n, ptr(cd), ptr(sd),
+                                                      1, k, stream()) == 0
+    want = A.copy()
+    want[:, 2, :] = c[:, None] * A[:, 2, :] + s[:, None] * A[:, 6, :]
+    want[:, 6, :] = c[:, None] * A[:, 6, :] - s[:, None] * A[:, 2, :]
+    assert np.abs(from_dev(Ad, k, m, n) - want).max() < tol
+    # right: columns 0 and 3
+    Ad = to_dev(A, dt)
+    base = ptr(Ad)
+    assert getattr(gbla_lib, f"gbla_{p}rot_batched")(m, base, 1, base + 3 * m * es, 1, m * n, ptr(cd), ptr(sd), 1,
+                                                      k, stream()) == 0
+    want = A.copy()
+    want[:, :, 0] = c[:, None] * A[:, :, 0] + s[:, None] * A[:, :, 3]
+    want[:, :, 3] = c[:, None] * A[:, :, 3] - s[:, None] * A[:, :, 0]
+    assert np.abs(from_dev(Ad, k, m, n) - want).max() < tol

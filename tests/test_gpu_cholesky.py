@@ -132,3 +132,77 @@ def test_d1_config_full_size_residual(gbla_lib, cuda):
     idx = np.arange(0, k, 64)
     _, xref, _ = O.posv(M[idx], b[idx])
     assert rel_err(x[idx], xref) < 1e-6
+
+
+# beyond 128: shared-memory working copy up to ~230 (f32) / ~160 (f64), then
+# factored in place in global memory
+BIG_NS = {np.float32: [129, 150, 200, 231, 300, 520], np.float64: [129, 150, 161, 200, 400]}
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("which", range(5))
+def test_big_potrf_potrs_vs_oracle(gbla_lib, cuda, dt, which):
+    """CholeskyBatchFactoriser::factorise + solve for n > 128 (cusolverDn
+    potrfBatched has no size cap, include/tensor.cuh:2135-2197)."""
+    n = BIG_NS[dt][which]
+    rng = np.random.default_rng(n)
+    k = 5
+    A = spd_batch(rng, k, n, shift=0.5)
+    Ad = to_dev(A, dt)
+    info = _potrf(gbla_lib, Ad, n, k, dt)
+    assert (info.cpu().numpy() == 0).all()
+    L = from_dev(Ad, k, n, n)
+    Lo, _ = O.potrf(A)
+    tol = 2e-6 if dt == np.float32 else 1e-13
+    assert rel_err(np.tril(L), np.tril(Lo)) < tol * np.sqrt(n)
+    assert np.array_equal(np.triu(L, 1), np.triu(A.astype(dt), 1))  # strict upper triangle untouched
+    b = rng.standard_normal((k, n, 3))
+    bd = to_dev(b, dt)
+    assert getattr(gbla_lib, f"gbla_{PFX[dt]}potrs_batched")(n, 3, ptr(Ad), n * n, ptr(bd), n * 3, k, stream()) == 0
+    _, xo, _ = O.posv(A, b)
+    kappa = max(np.linalg.cond(A[i]) for i in range(k))
+    assert rel_err(from_dev(bd, k, n, 3), xo) < tol * kappa * np.sqrt(n)
+
+
+@pytest.mark.parametrize("n,dt", [(150, np.float32), (200, np.float32), (231, np.float32), (140, np.float64),
+                                  (161, np.float64)])
+def test_big_posv_refined_vs_oracle(gbla_lib, cuda, n, dt):
+    """Fused factor + solve with refinement above n = 128 (the residual runs
+    over the whole original lower triangle, row by row)."""
+    import torch
+    rng = np.random.default_rng(n + 1)
+    k = 4
+    A = spd_batch(rng, k, n, shift=0.1)
+    A[:, np.triu_indices(n, 1)[0], np.triu_indices(n, 1)[1]] = 7.0  # upper triangle is never read
+    b = rng.standard_normal((k, n, 2))
+    Ad, bd = to_dev(A, dt), to_dev(b, dt)
+    info = torch.full((k,), -1, dtype=torch.int32, device="cuda")
+    assert getattr(gbla_lib, f"gbla_{PFX[dt]}posv_batched")(n, 2, ptr(Ad), n * n, ptr(bd), n * 2, ptr(info), 2, k,
+                                                             stream()) == 0
+    assert (info.cpu().numpy() == 0).all()
+    Afull = np.tril(A) + np.tril(A, -1).transpose(0, 2, 1)
+    _, xo, _ = O.posv(Afull, b)
+    assert rel_err(from_dev(bd, k, n, 2), xo) < (1e-6 if dt == np.float32 else 1e-13)
+
+
+def test_big_posv_global_memory_refinement_refused(gbla_lib, cuda):
+    import torch
+    n, k = 300, 2
+    A = spd_batch(np.random.default_rng(2), k, n, shift=0.5)
+    b = np.ones((k, n, 1))
+    Ad, bd = to_dev(A, np.float32), to_dev(b, np.float32)
+    info = torch.zeros(k, dtype=torch.int32, device="cuda")
+    assert gbla_lib.gbla_sposv_batched(n, 1, ptr(Ad), n * n, ptr(bd), n, ptr(info), 1, k, stream()) == 2
+    assert gbla_lib.gbla_sposv_batched(n, 1, ptr(Ad), n * n, ptr(bd), n, ptr(info), 0, k, stream()) == 0
+    _, xo, _ = O.posv(A, b)
+    assert rel_err(from_dev(bd, k, n, 1), xo) < 1e-3
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_big_not_positive_definite_info(gbla_lib, cuda, dt):
+    n = 300 if dt == np.float32 else 200   # global-memory variant
+    A = spd_batch(np.random.default_rng(4), 2, n, shift=0.5)
+    A[1, 57, 57] = -1e3                    # leading minor of order 58 is not positive definite
+    Ad = to_dev(A, dt)
+    info = _potrf(gbla_lib, Ad, n, 2, dt)
+    assert info.cpu().tolist() == [0, 58]

@@ -127,7 +127,10 @@ def test_d3_config_full_size(gbla_lib, cuda, dt):
 
 
 class Cfg(C.Structure):
-    _fields_ = [("bucket_width", C.c_int), ("large_threads", C.c_int), ("fork_small", C.c_int)]
+    _fields_ = [("threads", C.c_int), ("systems_per_block", C.c_int)]
+
+
+CONFIGS = [(128, 1), (128, 2), (256, 1), (256, 2), (256, 4), (512, 1), (512, 2), (512, 4), (512, 8)]
 
 
 def test_config_get_set_and_invalid(gbla_lib, cuda):
@@ -136,12 +139,15 @@ def test_config_get_set_and_invalid(gbla_lib, cuda):
     assert st == 0
     c = Cfg()
     assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(c)) == 0
-    assert (c.bucket_width, c.large_threads, c.fork_small) == (96, 256, 1)
-    for bad in (Cfg(17, 256, 1), Cfg(32, 96, 1), Cfg(32, 256, 2)):
+    assert (c.threads, c.systems_per_block) == (256, 2)
+    for bad in (Cfg(64, 1), Cfg(256, 3), Cfg(128, 4), Cfg(256, 8), Cfg(1024, 1)):
         assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(bad)) == 1
-    assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(Cfg(16, 512, 0))) == 0
+    assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(Cfg(512, 8))) == 0
     assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(c)) == 0
-    assert (c.bucket_width, c.large_threads, c.fork_small) == (16, 512, 0)
+    assert (c.threads, c.systems_per_block) == (512, 8)
+    ntasks, smem = C.c_int(), C.c_size_t()
+    assert gbla_lib.gbla_ragged_plan_tasks(p, C.byref(ntasks), C.byref(smem)) == 0
+    assert 0 < ntasks.value <= len(n) and 0 < smem.value <= 226 * 1024
     assert gbla_lib.gbla_ragged_plan_destroy(p) == 0
 
 
@@ -156,29 +162,57 @@ def test_every_configuration_gives_identical_results_and_autotune_keeps_inputs(g
     tune = gbla_lib.gbla_sragged_autotune if dt == np.float32 else gbla_lib.gbla_dragged_autotune
     refine = 1 if dt == np.float32 else 2
 
-    def run():
-        Ad, Bd = Ah.clone(), Bh.clone()
-        info = torch.full((len(n),), -1, dtype=torch.int32, device="cuda")
-        assert fn(p, Ad.data_ptr(), Bd.data_ptr(), info.data_ptr(), refine, stream()) == 0
-        torch.cuda.synchronize()
-        assert (info == 0).all()
+    def run(times=1):
+        for _ in range(times):  # repeated calls: the queue counter resets itself
+            Ad, Bd = Ah.clone(), Bh.clone()
+            info = torch.full((len(n),), -1, dtype=torch.int32, device="cuda")
+            assert fn(p, Ad.data_ptr(), Bd.data_ptr(), info.data_ptr(), refine, stream()) == 0
+            torch.cuda.synchronize()
+            assert (info == 0).all()
         return Ad, Bd
 
-    A0, X0 = run()
-    for cfg in (Cfg(48, 128, 0), Cfg(32, 512, 1), Cfg(16, 256, 1), Cfg(16, 64, 1)):
-        assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(cfg)) == 0
-        A1, X1 = run()
-        assert torch.equal(A1, A0) and torch.equal(X1, X0)
+    A0, X0 = run(3)
+    for cfg in CONFIGS:
+        assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(Cfg(*cfg))) == 0
+        A1, X1 = run(2)
+        assert torch.equal(A1, A0) and torch.equal(X1, X0), cfg
     Ak, Bk = Ah.clone(), Bh.clone()
     best, ms = Cfg(), C.c_float()
     assert tune(p, Ak.data_ptr(), Bk.data_ptr(), refine, 2, C.byref(best), C.byref(ms), stream()) == 0
     torch.cuda.synchronize()
     assert torch.equal(Ak, Ah) and torch.equal(Bk, Bh)       # inputs untouched
-    assert best.bucket_width in (96, 48, 32, 16) and best.large_threads in (64, 128, 256, 512) and ms.value > 0
+    assert (best.threads, best.systems_per_block) in CONFIGS and ms.value > 0
     cur = Cfg()
     assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(cur)) == 0
-    assert (cur.bucket_width, cur.large_threads, cur.fork_small) == (best.bucket_width, best.large_threads,
-                                                                   best.fork_small)
+    assert (cur.threads, cur.systems_per_block) == (best.threads, best.systems_per_block)
     A2, X2 = run()
     assert torch.equal(A2, A0) and torch.equal(X2, X0)
+    assert gbla_lib.gbla_ragged_plan_destroy(p) == 0
+
+
+def test_graph_replays_of_one_launch(gbla_lib, cuda):
+    """A call is one kernel; captured in a CUDA graph it replays correctly many
+    times in a row (the queue counter is reset by each launch)."""
+    import torch
+    n, nrhs, a_off, b_off, A, B = workloads.d3_ragged(count=2000, seed=9, dtype=np.float32)
+    st, p = _plan(gbla_lib, a_off, b_off, n, nrhs)
+    assert st == 0
+    A0, B0 = torch.tensor(A).cuda(), torch.tensor(B).cuda()
+    Ad, Bd = A0.clone(), B0.clone()
+    info = torch.full((len(n),), -1, dtype=torch.int32, device="cuda")
+    assert gbla_lib.gbla_sposv_ragged(p, Ad.data_ptr(), Bd.data_ptr(), info.data_ptr(), 1, stream()) == 0
+    torch.cuda.synchronize()
+    X_ref = Bd.clone()
+    g = torch.cuda.CUDAGraph()
+    cap = torch.cuda.Stream()
+    with torch.cuda.graph(g, stream=cap):
+        cs = torch.cuda.current_stream().cuda_stream
+        assert gbla_lib.gbla_sposv_ragged(p, Ad.data_ptr(), Bd.data_ptr(), info.data_ptr(), 1, cs) == 0
+    for _ in range(5):
+        Ad.copy_(A0)
+        Bd.copy_(B0)
+        info.fill_(-1)
+        g.replay()
+        torch.cuda.synchronize()
+        assert (info == 0).all() and torch.equal(Bd, X_ref)
     assert gbla_lib.gbla_ragged_plan_destroy(p) == 0
