@@ -648,7 +648,7 @@ def run_ours_d3(args, dev, st, L, rank, world, dist):
         tune = L.gbla_sragged_autotune if dt == np.float32 else L.gbla_dragged_autotune
         _lib.check(tune(plan, A0.data_ptr(), B0.data_ptr(), refine, 3, C.byref(best), C.byref(best_ms), st),
                    "autotune")
-        tuning.update({"chosen": best.as_dict(), "chosen_ms": best_ms.value, "candidates": 9})
+        tuning.update({"chosen": best.as_dict(), "chosen_ms": best_ms.value, "candidates": 13})
         cfg = best
     nsteps = args.warmup + args.steps
     As = [A0.clone() for _ in range(nsteps)]

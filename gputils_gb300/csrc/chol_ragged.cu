@@ -464,10 +464,11 @@ __device__ __forceinline__ void large_system(const RaggedSys &s, int nmax, unsig
 // Blocks pull tasks from the queue head ctr[0] until it passes ntasks; the
 // last block to finish (ctr[1]) resets both counters for the next call.  No
 // block waits on another: a block that finds the queue empty simply leaves.
-// 128 registers per thread whatever the block size (the lane-row path keeps a
-// 32-wide row and its refinement state in registers)
+// 128 registers per thread up to 512 threads (the lane-row path keeps a
+// 32-wide row and its refinement state in registers); 768 threads trade
+// registers (80 a thread) for 24 warps per SM
 template <typename T, int THREADS>
-__global__ void __launch_bounds__(THREADS, 512 / THREADS)
+__global__ void __launch_bounds__(THREADS, THREADS > 512 ? 1 : 512 / THREADS)
     k_ragged_persistent(const RaggedTask *__restrict__ tasks, int ntasks, const RaggedSys *__restrict__ sys,
                         int *__restrict__ ctr, T *__restrict__ A, T *__restrict__ B, int *__restrict__ info,
                         int refine) {
@@ -515,7 +516,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS)
 }
 
 static bool config_valid(const gbla_ragged_config &c) {
-    const bool t = c.threads == 128 || c.threads == 256 || c.threads == 512;
+    const bool t = c.threads == 128 || c.threads == 256 || c.threads == 512 || c.threads == 768;
     const bool g = c.systems_per_block == 1 || c.systems_per_block == 2 || c.systems_per_block == 4 ||
                    c.systems_per_block == 8;
     return t && g && c.systems_per_block * 64 <= c.threads;  // at least two warps per system
@@ -581,6 +582,7 @@ static gbla_status ragged_launch(const gbla_ragged_plan *p, T *A, T *B, int *inf
     if (dev != p->device) return GBLA_INVALID_VALUE;
     if (p->cfg.threads == 128) return launch_persistent<T, 128>(p, A, B, info, refine, st);
     if (p->cfg.threads == 512) return launch_persistent<T, 512>(p, A, B, info, refine, st);
+    if (p->cfg.threads == 768) return launch_persistent<T, 768>(p, A, B, info, refine, st);
     return launch_persistent<T, 256>(p, A, B, info, refine, st);
 }
 
@@ -616,8 +618,8 @@ static gbla_status ragged_autotune(gbla_ragged_plan *p, const T *A, const T *B, 
     const gbla_ragged_config saved = p->cfg;
     gbla_ragged_config best = saved;
     float best_t = 3.4e38f;
-    const int threads[3] = {128, 256, 512}, groups[4] = {1, 2, 4, 8};
-    for (int ti = 0; ti < 3 && status == GBLA_SUCCESS; ti++)
+    const int threads[4] = {128, 256, 512, 768}, groups[4] = {1, 2, 4, 8};
+    for (int ti = 0; ti < 4 && status == GBLA_SUCCESS; ti++)
         for (int gi = 0; gi < 4 && status == GBLA_SUCCESS; gi++) {
             const gbla_ragged_config c = {threads[ti], groups[gi]};
             if (!config_valid(c)) continue;

@@ -314,14 +314,49 @@ __global__ void __launch_bounds__(128, 1)
 // ------------------------------------------------------------ CTA kernel
 // One block of 256 threads per matrix: 32 column pairs x 8 lanes per pair,
 // rows split across the 8 lanes; A (m x n) and V (n x n) in shared memory.
-// Column strides are multiples of 32 words, so a word's bank is its row mod
-// 32, and the four 8-lane groups of a warp start their row walk 8 rows apart:
-// every shared access of a round is conflict-free.  Column norms are cached
+// Column strides are multiples of 32 words; a lane moves its rows of a
+// column as 16-byte vectors (svj_ld / svj_st: the 8 lanes of a group cover
+// 128 contiguous bytes, conflict-free), and the rows loaded for a pair's dot
+// product are the ones it rotates, so a rotated pair costs one load and one
+// store of each of its columns of A and V.  Column norms are cached
 // (recomputed from the columns at the start of every sweep, updated by
 // alpha - t gamma, beta + t gamma after a rotation), so a round computes one
 // dot product per pair.
 constexpr int SVJ_CTA_THREADS = 256;
 constexpr int SVJ_GROUP = 8;
+
+// Rows of one column held by lane gl of an 8-lane group, in 16-byte vectors:
+// rows E gl + 8 E s .. + E - 1 (E = 16 / sizeof(T) values per vector, s <
+// CNT / E).  Column strides are multiples of 32 words, so the 8 lanes of a
+// group read 128 contiguous bytes per vector and the four groups of a warp
+// (other columns) are served in separate phases: conflict-free.
+template <typename T, int CNT>
+__device__ __forceinline__ void svj_ld(const T *col, int gl, T (&x)[CNT]) {
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int s = 0; s < CNT / 4; s++) {
+            const float4 v = reinterpret_cast<const float4 *>(col)[gl + 8 * s];
+            x[4 * s] = v.x; x[4 * s + 1] = v.y; x[4 * s + 2] = v.z; x[4 * s + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < CNT / 2; s++) {
+            const double2 v = reinterpret_cast<const double2 *>(col)[gl + 8 * s];
+            x[2 * s] = v.x; x[2 * s + 1] = v.y;
+        }
+    }
+}
+template <typename T, int CNT>
+__device__ __forceinline__ void svj_st(T *col, int gl, const T (&x)[CNT]) {
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int s = 0; s < CNT / 4; s++)
+            reinterpret_cast<float4 *>(col)[gl + 8 * s] = make_float4(x[4 * s], x[4 * s + 1], x[4 * s + 2], x[4 * s + 3]);
+    } else {
+#pragma unroll
+        for (int s = 0; s < CNT / 2; s++) reinterpret_cast<double2 *>(col)[gl + 8 * s] = make_double2(x[2 * s], x[2 * s + 1]);
+    }
+}
 
 // MR, NR: row counts of A and V padded to 32, 64 or 128 (compile time).  The
 // padding rows hold zeros, which every rotation maps to zeros, so the row
@@ -343,9 +378,7 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
     T *nrm = rinv + n;                // n: cached |a_j|^2
     const int tid = threadIdx.x, g = tid / SVJ_GROUP, gl = tid % SVJ_GROUP;
     const int N = n + (n & 1), M = N - 1;
-    const int rot = 8 * (g & 3);
-    const int w0 = gl + rot;  // < 32 <= MR, NR
-    constexpr int MT = MR / 8, NT = NR / 8;
+    constexpr int MT = MR / 8, NT = NR / 8;  // rows of a column per lane
 
     for (int64_t mat = blockIdx.x; mat < batch; mat += gridDim.x) {
         const T *ag = A + mat * sA;
@@ -409,12 +442,10 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
                 const int j = j0 + g;
                 T f = 0.f;
                 if (j < n) {
-                    const T *col = a + j * lda;
+                    T x[MT];
+                    svj_ld<T, MT>(a + j * lda, gl, x);
 #pragma unroll
-                    for (int t = 0; t < MT; t++) {
-                        const T x = col[(w0 + 8 * t) & (MR - 1)];
-                        f = fma(x, x, f);
-                    }
+                    for (int t = 0; t < MT; t++) f = fma(x[t], x[t], f);
                 }
                 f = group_sum(f, SVJ_GROUP);
                 if (gl == 0 && j < n) nrm[j] = f;
@@ -439,12 +470,12 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
                 const bool act = q >= 0 && q < n;
                 T gamma = 0.f, alpha = 0.f, beta = 0.f;
                 T *ap = a + (act ? p : 0) * lda, *aq = a + (act ? q : 0) * lda;
+                T xa[MT], xb[MT];  // the pair's rows of this lane, kept for the rotation
                 if (act) {
+                    svj_ld<T, MT>(ap, gl, xa);
+                    svj_ld<T, MT>(aq, gl, xb);
 #pragma unroll
-                    for (int t = 0; t < MT; t++) {
-                        const int i = (w0 + 8 * t) & (MR - 1);
-                        gamma = fma(ap[i], aq[i], gamma);
-                    }
+                    for (int t = 0; t < MT; t++) gamma = fma(xa[t], xb[t], gamma);
                     alpha = nrm[p];
                     beta = nrm[q];
                 }
@@ -454,19 +485,24 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
                     rotated = 1;
 #pragma unroll
                     for (int t = 0; t < MT; t++) {
-                        const int i = (w0 + 8 * t) & (MR - 1);
-                        const T x = ap[i], y = aq[i];
-                        ap[i] = fma(c, x, -sn * y);
-                        aq[i] = fma(sn, x, c * y);
+                        const T x = xa[t], y = xb[t];
+                        xa[t] = fma(c, x, -sn * y);
+                        xb[t] = fma(sn, x, c * y);
                     }
+                    svj_st<T, MT>(ap, gl, xa);
+                    svj_st<T, MT>(aq, gl, xb);
                     T *vp = v + p * ldv, *vq = v + q * ldv;
+                    T ya[NT], yb[NT];
+                    svj_ld<T, NT>(vp, gl, ya);
+                    svj_ld<T, NT>(vq, gl, yb);
 #pragma unroll
                     for (int t = 0; t < NT; t++) {
-                        const int i = (w0 + 8 * t) & (NR - 1);
-                        const T x = vp[i], y = vq[i];
-                        vp[i] = fma(c, x, -sn * y);
-                        vq[i] = fma(sn, x, c * y);
+                        const T x = ya[t], y = yb[t];
+                        ya[t] = fma(c, x, -sn * y);
+                        yb[t] = fma(sn, x, c * y);
                     }
+                    svj_st<T, NT>(vp, gl, ya);
+                    svj_st<T, NT>(vq, gl, yb);
                     if (gl == 0) {
                         nrm[p] = fma(-tn, gamma, alpha);
                         nrm[q] = fma(tn, gamma, beta);

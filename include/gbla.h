@@ -128,9 +128,10 @@ gbla_status gbla_ragged_plan_create(const int64_t *a_offsets, const int64_t *b_o
                                     const int *nrhs, int count, gbla_ragged_plan **plan);
 gbla_status gbla_ragged_plan_destroy(gbla_ragged_plan *plan);
 
-/* Launch configuration of a plan: threads per block (128, 256, 512) and the
- * most systems with n > 32 that one block factors at once (1, 2, 4, 8; at
- * most threads / 64), each with threads / 32 / count warps and its own
+/* Launch configuration of a plan: threads per block (128, 256, 512 with 128
+ * registers a thread, or 768 with 80) and the most systems with n > 32 that
+ * one block factors at once (1, 2, 4, 8; at most threads / 64), each with
+ * threads / 32 / count warps and its own
  * shared-memory slot (sized for the group's largest system; the block's
  * shared memory -- and so the blocks per SM -- is that many slots of the
  * plan's largest system).  Systems with n <= 32 run the lane-row method,
@@ -151,7 +152,7 @@ gbla_status gbla_ragged_plan_set_config(gbla_ragged_plan *plan, const gbla_ragge
 gbla_status gbla_ragged_plan_tasks(const gbla_ragged_plan *plan, int *ntasks, size_t *smem_bytes);
 
 /* Autotuner: times every valid configuration (threads x systems per block,
- * 9 candidates) on this batch -- best of `reps` runs after a warm-up, each on
+ * 13 candidates) on this batch -- best of `reps` runs after a warm-up, each on
  * fresh copies of A and B -- and keeps the fastest in the plan.  A and B are
  * not modified.  best / best_ms (nullable) receive the choice and its time.
  * Allocates scratch copies and synchronises: a set-up call. */

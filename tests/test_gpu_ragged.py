@@ -130,7 +130,8 @@ class Cfg(C.Structure):
     _fields_ = [("threads", C.c_int), ("systems_per_block", C.c_int)]
 
 
-CONFIGS = [(128, 1), (128, 2), (256, 1), (256, 2), (256, 4), (512, 1), (512, 2), (512, 4), (512, 8)]
+CONFIGS = [(128, 1), (128, 2), (256, 1), (256, 2), (256, 4), (512, 1), (512, 2), (512, 4), (512, 8), (768, 1),
+           (768, 2), (768, 4), (768, 8)]
 
 
 def test_config_get_set_and_invalid(gbla_lib, cuda):
@@ -140,7 +141,7 @@ def test_config_get_set_and_invalid(gbla_lib, cuda):
     c = Cfg()
     assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(c)) == 0
     assert (c.threads, c.systems_per_block) == (256, 2)
-    for bad in (Cfg(64, 1), Cfg(256, 3), Cfg(128, 4), Cfg(256, 8), Cfg(1024, 1)):
+    for bad in (Cfg(64, 1), Cfg(256, 3), Cfg(128, 4), Cfg(256, 8), Cfg(1024, 1), Cfg(768, 16)):
         assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(bad)) == 1
     assert gbla_lib.gbla_ragged_plan_set_config(p, C.byref(Cfg(512, 8))) == 0
     assert gbla_lib.gbla_ragged_plan_get_config(p, C.byref(c)) == 0
