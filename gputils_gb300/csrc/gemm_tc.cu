@@ -17,10 +17,12 @@
 //   (64 KB each, one pair-of-pairs); all warps: raw stage -> split -> BF16
 //   operand tiles (K-major core-matrix layout, no swizzle); fence.proxy.async;
 //   barrier; the stage is refilled with the pair-of-pairs two steps ahead; one
-//   thread issues the 24 tcgen05.mma and commits to an mbarrier; all warps
-//   wait (bounded), read their TMEM rows with tcgen05.ld and store C.  Every
-//   wait is bounded; on a timeout the block records an error flag, waits for
-//   its copies, frees its TMEM and exits.
+//   thread issues the 24 tcgen05.mma into one of two TMEM accumulators and
+//   commits to an mbarrier.  Once the MMAs of pair-of-pairs q are done, the
+//   warps split q + grid and issue its MMAs into the other accumulator, then
+//   read q's accumulator with tcgen05.ld and store C while those MMAs run.
+//   Every wait is bounded; on a timeout the block records an error flag, waits
+//   for its copies, frees its TMEM and exits.
 #include <cuda_bf16.h>
 #include "common.cuh"
 
@@ -31,7 +33,7 @@ constexpr int TC_TILE_BYTES = 128 * 64 * 2;    // one operand split: 128 rows x 
 constexpr int TC_RAW_BYTES = 4 * 64 * 64 * 4;   // fp32 A_i, A_j, B_i, B_j of one pair-of-pairs = 64 KB
 // A and B, 3 splits each; two raw fp32 stages; barrier
 constexpr int TC_SMEM = 6 * TC_TILE_BYTES + 2 * TC_RAW_BYTES + 64;
-constexpr int TC_TMEM_COLS = 128;
+constexpr int TC_TMEM_COLS = 256;  // two 128-column accumulators
 constexpr uint32_t TC_SPIN_LIMIT = 1u << 26;
 
 __device__ int g_tc_error = 0;
@@ -179,41 +181,34 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     };
     issue_raw(blockIdx.x, 0);
     issue_raw(blockIdx.x + gridDim.x, 1);
-    int stage = 0;
-    for (int q = blockIdx.x; q < npp; q += gridDim.x, stage ^= 1) {
-        const int p0 = 2 * q;
-        const bool has1 = p0 + 1 < batch;
-        asm volatile("cp.async.wait_group 1;" ::: "memory");  // this stage landed; the other may be in flight
-        __syncthreads();
-        // ---- split: raw fp32 (shared) -> three BF16 K-major operand tiles
-        {
-            const unsigned char *rs = raw0 + stage * TC_RAW_BYTES;
+    // split: raw fp32 (shared) -> three BF16 K-major operand tiles
+    auto split = [&](int stg) {
+        const unsigned char *rs = raw0 + stg * TC_RAW_BYTES;
 #pragma unroll
-            for (int it = 0; it < 4; it++) {
-                const int item = tid + it * TC_THREADS;  // 0..1023 = 128 rows x 8 kgroups
-                const int row = item & 127, kg = item >> 7;
-                const int half = row >> 6, r = row & 63;
-                const float *ra = reinterpret_cast<const float *>(rs + half * 16384);
-                float va[8], vb[8];
+        for (int it = 0; it < 4; it++) {
+            const int item = tid + it * TC_THREADS;  // 0..1023 = 128 rows x 8 kgroups
+            const int row = item & 127, kg = item >> 7;
+            const int half = row >> 6, r = row & 63;
+            const float *ra = reinterpret_cast<const float *>(rs + half * 16384);
+            float va[8], vb[8];
 #pragma unroll
-                for (int e = 0; e < 8; e++) va[e] = ra[(kg * 8 + e) * 64 + r];
-                const unsigned char *rb = rs + 32768 + half * 16384 + r * 256;
-                const float4 b0 = *reinterpret_cast<const float4 *>(rb + (((2 * kg) ^ (r & 7)) << 4));
-                const float4 b1 = *reinterpret_cast<const float4 *>(rb + (((2 * kg + 1) ^ (r & 7)) << 4));
-                vb[0] = b0.x; vb[1] = b0.y; vb[2] = b0.z; vb[3] = b0.w;
-                vb[4] = b1.x; vb[5] = b1.y; vb[6] = b1.z; vb[7] = b1.w;
-                const uint32_t off = kmajor_off(row, kg);
-                store_split_row(sAop, off, va);
-                store_split_row(sBop, off, vb);
-            }
+            for (int e = 0; e < 8; e++) va[e] = ra[(kg * 8 + e) * 64 + r];
+            const unsigned char *rb = rs + 32768 + half * 16384 + r * 256;
+            const float4 b0 = *reinterpret_cast<const float4 *>(rb + (((2 * kg) ^ (r & 7)) << 4));
+            const float4 b1 = *reinterpret_cast<const float4 *>(rb + (((2 * kg + 1) ^ (r & 7)) << 4));
+            vb[0] = b0.x; vb[1] = b0.y; vb[2] = b0.z; vb[3] = b0.w;
+            vb[4] = b1.x; vb[5] = b1.y; vb[6] = b1.z; vb[7] = b1.w;
+            const uint32_t off = kmajor_off(row, kg);
+            store_split_row(sAop, off, va);
+            store_split_row(sBop, off, vb);
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        // this stage is consumed: start the copies of the pair-of-pairs two steps ahead
-        issue_raw(q + 2 * gridDim.x, stage);
+    };
+    // one thread issues the 24 MMAs of a pair-of-pairs into accumulator buffer buf
+    auto issue_mma = [&](int buf) {
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t a0 = smem_u32(sAop), b0 = smem_u32(sBop);
+            const uint32_t d = tmem + (uint32_t)(buf * 128);
             uint32_t acc = 0;
 #pragma unroll
             for (int s = 0; s < 4; s++) {  // K slices of 16
@@ -225,13 +220,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int p = 0; p < 6; p++) {
                     uint64_t ad = make_desc(a0 + pa[p] * TC_TILE_BYTES + ko);
                     uint64_t bd = make_desc(b0 + pb[p] * TC_TILE_BYTES + ko);
-                    mma_bf16(tmem, ad, bd, idesc, acc);
+                    mma_bf16(d, ad, bd, idesc, acc);
                     acc = 1;
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a)
                          : "memory");
         }
+    };
+    // Accumulators are double-buffered in tensor memory (2 x 128 columns): the
+    // MMAs of pair-of-pairs q + grid run while the epilogue of q reads its
+    // buffer.  The operand tiles are single-buffered, so the split of q + grid
+    // waits for the MMAs of q.
+    int stage = 0, buf = 0;
+    const int q0 = blockIdx.x;
+    if (q0 < npp) {
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        __syncthreads();
+        split(stage);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        issue_raw(q0 + 2 * gridDim.x, stage);
+        issue_mma(buf);
+    }
+    for (int q = q0; q < npp; q += gridDim.x) {
+        const int p0 = 2 * q;
+        const bool has1 = p0 + 1 < batch;
+        // the MMAs of q are done: its accumulator is ready and the operand tiles are free
         bool ok = mbar_wait(bar_a, phase);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) { atomicExch(&g_tc_error, 1); s_abort = 1; }
@@ -239,14 +254,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         phase ^= 1;
         asm volatile("tcgen05.fence::after_thread_sync;");
-        // ---- epilogue: warp w reads lanes 32*(w%4).., 32 columns of its pair's diagonal block
+        const int qn = q + gridDim.x;
+        if (qn < npp) {
+            stage ^= 1;
+            asm volatile("cp.async.wait_group 1;" ::: "memory");  // qn's stage landed; the other may be in flight
+            __syncthreads();
+            split(stage);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            // this stage is consumed: start the copies of the pair-of-pairs two steps ahead
+            issue_raw(qn + 2 * gridDim.x, stage);
+            issue_mma(buf ^ 1);
+        }
+        // ---- epilogue of q (buffer buf): warp w reads lanes 32*(w%4).., 32 columns of its pair's diagonal block
         {
             const int quad = warp & 3, half = warp >> 2;
             const int row = quad * 32 + lane;          // D row = TMEM lane
             const int pair = p0 + (row >> 6);
             const int col0 = (row >> 6) * 64 + half * 32;  // diagonal block, 32 of its 64 columns
             uint32_t v[32];
-            uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)col0;
+            uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * 128 + col0);
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -269,8 +296,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
             }
         }
+        // every read of buffer buf is done before the MMAs of q + 2 grid overwrite it
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
+        buf ^= 1;
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy may land after the block is gone
     __syncthreads();
