@@ -363,7 +363,7 @@ __device__ __forceinline__ void svj_st(T *col, int gl, const T (&x)[CNT]) {
 // loops need no bounds tests and unroll completely; a lane walks rows
 // (gl + rot + 8 t) mod MR.
 template <typename T, int MR, int NR>
-__global__ void __launch_bounds__(SVJ_CTA_THREADS, 3)
+__global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
     k_gesvj_cta(int m, int n, const T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
                 T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
                 int64_t sV0, T tol, int max_sweeps, int warm_budget, int *__restrict__ fallback_out,
