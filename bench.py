@@ -80,6 +80,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-workloads", action="store_true",
                     help="d2: skip the other configurations' results in the default line")
     ap.add_argument("--no-autotune", action="store_true", help="d3: keep the plan's default launch configuration")
+    ap.add_argument("--ragged-config", default=None,
+                    help="d3: threads,systems_per_block of the plan instead of autotuning (e.g. 768,8)")
     ap.add_argument("--ws-pairs", type=int, default=200_000, help="d5: (A, V) training pairs of the warm-start net")
     ap.add_argument("--ws-epochs", type=int, default=20, help="d5: training epochs of the warm-start net")
     return ap.parse_args(argv)
@@ -643,7 +645,12 @@ def run_ours_d3(args, dev, st, L, rank, world, dist):
     cfg = RaggedCfg()
     _lib.check(L.gbla_ragged_plan_get_config(plan, C.byref(cfg)), "get config")
     tuning = {"default": cfg.as_dict()}
-    if not args.no_autotune:
+    if args.ragged_config:
+        t, g = (int(v) for v in args.ragged_config.split(","))
+        cfg = RaggedCfg(t, g)
+        _lib.check(L.gbla_ragged_plan_set_config(plan, C.byref(cfg)), "set config")
+        tuning["set"] = cfg.as_dict()
+    elif not args.no_autotune:
         best, best_ms = RaggedCfg(), C.c_float()
         tune = L.gbla_sragged_autotune if dt == np.float32 else L.gbla_dragged_autotune
         _lib.check(tune(plan, A0.data_ptr(), B0.data_ptr(), refine, 3, C.byref(best), C.byref(best_ms), st),
