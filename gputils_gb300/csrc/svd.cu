@@ -3,8 +3,10 @@
 // Replaces Svd<T>::factorise (a host loop of cusolverDn<t>gesvd, one call per
 // matrix) and k_countNonzeroSingularValues.  The columns of A are rotated
 // pairwise until they are mutually orthogonal; V accumulates the rotations.
-// Pairs follow the round-robin (circle) tournament, so every round rotates
-// N/2 disjoint column pairs in parallel and a sweep is N-1 rounds.  A pair
+// Every round rotates disjoint column pairs in parallel and a sweep meets
+// every pair once: the warp kernel follows the round-robin (circle)
+// tournament (N-1 rounds), the block kernel a recursive halving of the
+// columns (NP-1 rounds, NP = n rounded up to a power of two).  A pair
 // (p < q) is rotated when |a_p . a_q| > tol ||a_p|| ||a_q|| with the
 // Rutishauser formulas (zeta = (|a_q|^2 - |a_p|^2) / (2 a_p.a_q),
 // t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2))); the sweep loop ends after a
@@ -312,58 +314,76 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // ------------------------------------------------------------ CTA kernel
-// One block of 256 threads per matrix: 32 column pairs x 8 lanes per pair,
-// rows split across the 8 lanes; A (m x n) and V (n x n) in shared memory.
+// One block per matrix: 32 column pairs x GL lanes per pair (GL = 4 or 8),
+// rows split across the GL lanes; A (m x n) and V (n x n) in shared memory.
 // Column strides are multiples of 32 words; a lane moves its rows of a
-// column as 16-byte vectors (svj_ld / svj_st: the 8 lanes of a group cover
-// 128 contiguous bytes, conflict-free), and the rows loaded for a pair's dot
-// product are the ones it rotates, so a rotated pair costs one load and one
-// store of each of its columns of A and V.  Column norms are cached
+// column as 16-byte vectors (svj_ld / svj_st, conflict-free).  The pair
+// ordering keeps one column of each pair (of A and of V) in the group's
+// registers for a whole phase of rounds, so a round loads the partner column
+// of A and, when the pair is rotated, stores it and loads and stores the
+// partner column of V: half the shared-memory traffic of moving both columns,
+// which bounds the kernel while most pairs rotate.  Column norms are cached
 // (recomputed from the columns at the start of every sweep, updated by
 // alpha - t gamma, beta + t gamma after a rotation), so a round computes one
 // dot product per pair.
-constexpr int SVJ_CTA_THREADS = 256;
-constexpr int SVJ_GROUP = 8;
 
-// Rows of one column held by lane gl of an 8-lane group, in 16-byte vectors:
-// rows E gl + 8 E s .. + E - 1 (E = 16 / sizeof(T) values per vector, s <
-// CNT / E).  Column strides are multiples of 32 words, so the 8 lanes of a
-// group read 128 contiguous bytes per vector and the four groups of a warp
-// (other columns) are served in separate phases: conflict-free.
-template <typename T, int CNT>
-__device__ __forceinline__ void svj_ld(const T *col, int gl, T (&x)[CNT]) {
+// Rows of one column held by lane gl of a GL-lane group (GL = 8 or 4), in
+// 16-byte vectors: rows E v .. E v + E - 1 (E = 16 / sizeof(T) values per
+// vector) for the vectors v = gl + GL s' (s' < CNT / E), where s' = s for
+// even groups (sw = 0) and s ^ 1 for odd ones (sw = 1, GL = 4 only).  Column
+// strides are multiples of 32 words, so with GL = 8 the group reads 128
+// contiguous bytes per vector (one bank each) and the four groups of a warp
+// (other columns) are served in separate phases; with GL = 4 the two groups
+// that share a phase read opposite halves of the banks: conflict-free.
+template <typename T, int CNT, int GL>
+__device__ __forceinline__ void svj_ld(const T *col, int gl, int sw, T (&x)[CNT]) {
     if constexpr (sizeof(T) == 4) {
 #pragma unroll
         for (int s = 0; s < CNT / 4; s++) {
-            const float4 v = reinterpret_cast<const float4 *>(col)[gl + 8 * s];
+            const float4 v = reinterpret_cast<const float4 *>(col)[gl + GL * (s ^ sw)];
             x[4 * s] = v.x; x[4 * s + 1] = v.y; x[4 * s + 2] = v.z; x[4 * s + 3] = v.w;
         }
     } else {
 #pragma unroll
         for (int s = 0; s < CNT / 2; s++) {
-            const double2 v = reinterpret_cast<const double2 *>(col)[gl + 8 * s];
+            const double2 v = reinterpret_cast<const double2 *>(col)[gl + GL * (s ^ sw)];
             x[2 * s] = v.x; x[2 * s + 1] = v.y;
         }
     }
 }
-template <typename T, int CNT>
-__device__ __forceinline__ void svj_st(T *col, int gl, const T (&x)[CNT]) {
+template <typename T, int CNT, int GL>
+__device__ __forceinline__ void svj_st(T *col, int gl, int sw, const T (&x)[CNT]) {
     if constexpr (sizeof(T) == 4) {
 #pragma unroll
         for (int s = 0; s < CNT / 4; s++)
-            reinterpret_cast<float4 *>(col)[gl + 8 * s] = make_float4(x[4 * s], x[4 * s + 1], x[4 * s + 2], x[4 * s + 3]);
+            reinterpret_cast<float4 *>(col)[gl + GL * (s ^ sw)] =
+                make_float4(x[4 * s], x[4 * s + 1], x[4 * s + 2], x[4 * s + 3]);
     } else {
 #pragma unroll
-        for (int s = 0; s < CNT / 2; s++) reinterpret_cast<double2 *>(col)[gl + 8 * s] = make_double2(x[2 * s], x[2 * s + 1]);
+        for (int s = 0; s < CNT / 2; s++)
+            reinterpret_cast<double2 *>(col)[gl + GL * (s ^ sw)] = make_double2(x[2 * s], x[2 * s + 1]);
     }
+}
+
+// Lanes per column pair: 4 for single precision up to 64 rows (16 rows a
+// lane, one 128-thread block per matrix, four blocks per SM), otherwise 8
+// (256 threads).  Fewer lanes per pair means fewer warp instructions per
+// pair (the pair's indices, the reduction and the angle are computed once
+// per group).  The register budgets keep the stationary and the moving
+// column of A and of V in registers without spilling.
+template <typename T, int MR>
+constexpr int svj_group() { return (sizeof(T) == 4 && MR <= 64) ? 4 : 8; }
+template <typename T, int MR>
+constexpr int svj_min_blocks() {
+    return sizeof(T) == 8 ? 2 : (svj_group<T, MR>() == 4 ? 4 : 2);
 }
 
 // MR, NR: row counts of A and V padded to 32, 64 or 128 (compile time).  The
 // padding rows hold zeros, which every rotation maps to zeros, so the row
-// loops need no bounds tests and unroll completely; a lane walks rows
-// (gl + rot + 8 t) mod MR.
-template <typename T, int MR, int NR>
-__global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
+// loops need no bounds tests and unroll completely.  32 groups of GL lanes
+// (one per column pair of a round).
+template <typename T, int MR, int NR, int GL = svj_group<T, MR>()>
+__global__ void __launch_bounds__(32 * GL, svj_min_blocks<T, MR>())
     k_gesvj_cta(int m, int n, const T *__restrict__ A, int64_t sA, T *__restrict__ S, int64_t sS,
                 T *__restrict__ Vt, int64_t sVt, T *__restrict__ U, int64_t sU, const T *__restrict__ V0,
                 int64_t sV0, T tol, int max_sweeps, int warm_budget, int *__restrict__ fallback_out,
@@ -376,33 +396,35 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
     T *sig = v + (size_t)n * ldv;     // n
     T *rinv = sig + n;                // n: 1 / |rotated column j|
     T *nrm = rinv + n;                // n: cached |a_j|^2
-    const int tid = threadIdx.x, g = tid / SVJ_GROUP, gl = tid % SVJ_GROUP;
-    const int N = n + (n & 1), M = N - 1;
-    constexpr int MT = MR / 8, NT = NR / 8;  // rows of a column per lane
+    constexpr int THREADS = 32 * GL;
+    const int tid = threadIdx.x, g = tid / GL, gl = tid % GL, sw = GL == 4 ? (g & 1) : 0;
+    int NP = 2;  // players of the round ordering: n rounded up to a power of two (<= 64)
+    while (NP < n) NP <<= 1;
+    constexpr int MT = MR / GL, NT = NR / GL;  // rows of a column per lane
 
     for (int64_t mat = blockIdx.x; mat < batch; mat += gridDim.x) {
         const T *ag = A + mat * sA;
-        for (int e = tid; e < MR * n; e += SVJ_CTA_THREADS) {
+        for (int e = tid; e < MR * n; e += THREADS) {
             const int i = e % MR, j = e / MR;
             a[j * lda + i] = i < m ? ag[(int64_t)j * m + i] : T(0);
         }
-        for (int e = tid; e < NR * n; e += SVJ_CTA_THREADS) {
+        for (int e = tid; e < NR * n; e += THREADS) {
             const int i = e % NR, j = e / NR;
             v[j * ldv + i] = i >= n ? T(0) : V0 ? V0[mat * sV0 + (int64_t)j * n + i] : (i == j ? T(1) : T(0));
         }
         __syncthreads();
         if (V0) {
             // A <- A V0, column by column through registers (rows by thread)
-            for (int i0 = 0; i0 < m; i0 += SVJ_CTA_THREADS / 4) {
+            for (int i0 = 0; i0 < m; i0 += THREADS / 4) {
                 // each thread: row i0 + tid % 64, columns j = tid / 64 + 4 t
-                const int i = i0 + tid % (SVJ_CTA_THREADS / 4);
+                const int i = i0 + tid % (THREADS / 4);
                 T acc[16];
                 for (int t = 0; t < 16; t++) acc[t] = 0.f;
                 if (i < m) {
                     for (int k = 0; k < n; k++) {
                         T aik = a[k * lda + i];
                         for (int t = 0; t < 16; t++) {
-                            int j = tid / (SVJ_CTA_THREADS / 4) + 4 * t;
+                            int j = tid / (THREADS / 4) + 4 * t;
                             if (j < n) acc[t] = fma(aik, v[j * ldv + k], acc[t]);
                         }
                     }
@@ -410,7 +432,7 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
                 __syncthreads();
                 if (i < m)
                     for (int t = 0; t < 16; t++) {
-                        int j = tid / (SVJ_CTA_THREADS / 4) + 4 * t;
+                        int j = tid / (THREADS / 4) + 4 * t;
                         if (j < n) a[j * lda + i] = acc[t];
                     }
                 __syncthreads();
@@ -438,75 +460,86 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
             // refresh the cached norms: group g takes columns g, g + 32.  The
             // trip count is the same for every lane (the group sum shuffles
             // across the whole warp); columns past n contribute nothing.
-            for (int j0 = 0; j0 < n; j0 += SVJ_CTA_THREADS / SVJ_GROUP) {
+            for (int j0 = 0; j0 < n; j0 += THREADS / GL) {
                 const int j = j0 + g;
                 T f = 0.f;
                 if (j < n) {
                     T x[MT];
-                    svj_ld<T, MT>(a + j * lda, gl, x);
+                    svj_ld<T, MT, GL>(a + j * lda, gl, sw, x);
 #pragma unroll
                     for (int t = 0; t < MT; t++) f = fma(x[t], x[t], f);
                 }
-                f = group_sum(f, SVJ_GROUP);
+                f = group_sum(f, GL);
                 if (gl == 0 && j < n) nrm[j] = f;
             }
             __syncthreads();
-            for (int r = 0; r < M; r++) {
-                int p = -1, q = -1;
-                if (g < N / 2) {
-                    int x, y;
-                    if (g == 0) {
-                        x = M;
-                        y = r;
-                    } else {
-                        x = r + g;
-                        if (x >= M) x -= M;
-                        y = r - g;
-                        if (y < 0) y += M;
-                    }
-                    p = x < y ? x : y;
-                    q = x < y ? y : x;
+            // Rounds: recursive halving of NP = 2^k >= n players.  A phase with
+            // half-size h splits the players into blocks of 2h; group g = (b, i)
+            // (b = g / h, i = g % h) keeps player b 2h + i (stationary, in
+            // registers for the whole phase) and meets the players b 2h + h +
+            // ((i + r) mod h) of the block's upper half in rounds r < h, which
+            // arrive through shared memory.  Phases h = NP/2, ..., 1 meet every
+            // pair once in NP - 1 rounds, and a round moves one column of A (and
+            // of V when rotated) per group instead of two.
+            for (int h = NP / 2; h >= 1; h >>= 1) {
+                const int b = g / h, i = g % h;
+                const int sc = b * 2 * h + i;  // stationary column
+                const bool s_ok = g < NP / 2 && sc < n;
+                T sa[MT], sv[NT], s_nrm = T(0);
+                if (s_ok) {
+                    svj_ld<T, MT, GL>(a + sc * lda, gl, sw, sa);
+                    svj_ld<T, NT, GL>(v + sc * ldv, gl, sw, sv);
+                    s_nrm = nrm[sc];
                 }
-                const bool act = q >= 0 && q < n;
-                T gamma = 0.f, alpha = 0.f, beta = 0.f;
-                T *ap = a + (act ? p : 0) * lda, *aq = a + (act ? q : 0) * lda;
-                T xa[MT], xb[MT];  // the pair's rows of this lane, kept for the rotation
-                if (act) {
-                    svj_ld<T, MT>(ap, gl, xa);
-                    svj_ld<T, MT>(aq, gl, xb);
+                bool s_dirty = false;
+                for (int r = 0; r < h; r++) {
+                    const int mc = b * 2 * h + h + ((i + r) & (h - 1));  // moving column
+                    const bool act = s_ok && mc < n;
+                    T gamma = T(0), g2 = T(0), beta = T(0);
+                    T *am = a + (act ? mc : 0) * lda;
+                    T xm[MT];
+                    if (act) {
+                        svj_ld<T, MT, GL>(am, gl, sw, xm);
 #pragma unroll
-                    for (int t = 0; t < MT; t++) gamma = fma(xa[t], xb[t], gamma);
-                    alpha = nrm[p];
-                    beta = nrm[q];
+                        for (int t = 0; t < MT; t += 2) {
+                            gamma = fma(sa[t], xm[t], gamma);
+                            g2 = fma(sa[t + 1], xm[t + 1], g2);
+                        }
+                        beta = nrm[mc];
+                    }
+                    gamma = group_sum(gamma + g2, GL);
+                    T c, sn, tn;
+                    if (act && jacobi_rotation_t<T>(s_nrm, beta, gamma, tol_eff, small, c, sn, tn)) {
+                        rotated = 1;
+                        s_dirty = true;
+#pragma unroll
+                        for (int t = 0; t < MT; t++) {
+                            const T x = sa[t], y = xm[t];
+                            sa[t] = fma(c, x, -sn * y);
+                            xm[t] = fma(sn, x, c * y);
+                        }
+                        svj_st<T, MT, GL>(am, gl, sw, xm);
+                        T *vm = v + mc * ldv;
+                        T ym[NT];
+                        svj_ld<T, NT, GL>(vm, gl, sw, ym);
+#pragma unroll
+                        for (int t = 0; t < NT; t++) {
+                            const T x = sv[t], y = ym[t];
+                            sv[t] = fma(c, x, -sn * y);
+                            ym[t] = fma(sn, x, c * y);
+                        }
+                        svj_st<T, NT, GL>(vm, gl, sw, ym);
+                        const T alpha = s_nrm;
+                        s_nrm = fma(-tn, gamma, alpha);
+                        if (gl == 0) nrm[mc] = fma(tn, gamma, beta);
+                    }
+                    __syncthreads();
                 }
-                gamma = group_sum(gamma, SVJ_GROUP);
-                T c, sn, tn;
-                if (act && jacobi_rotation_t<T>(alpha, beta, gamma, tol_eff, small, c, sn, tn)) {
-                    rotated = 1;
-#pragma unroll
-                    for (int t = 0; t < MT; t++) {
-                        const T x = xa[t], y = xb[t];
-                        xa[t] = fma(c, x, -sn * y);
-                        xb[t] = fma(sn, x, c * y);
-                    }
-                    svj_st<T, MT>(ap, gl, xa);
-                    svj_st<T, MT>(aq, gl, xb);
-                    T *vp = v + p * ldv, *vq = v + q * ldv;
-                    T ya[NT], yb[NT];
-                    svj_ld<T, NT>(vp, gl, ya);
-                    svj_ld<T, NT>(vq, gl, yb);
-#pragma unroll
-                    for (int t = 0; t < NT; t++) {
-                        const T x = ya[t], y = yb[t];
-                        ya[t] = fma(c, x, -sn * y);
-                        yb[t] = fma(sn, x, c * y);
-                    }
-                    svj_st<T, NT>(vp, gl, ya);
-                    svj_st<T, NT>(vq, gl, yb);
-                    if (gl == 0) {
-                        nrm[p] = fma(-tn, gamma, alpha);
-                        nrm[q] = fma(tn, gamma, beta);
-                    }
+                // the stationary column goes back before the next phase regroups the players
+                if (s_dirty) {
+                    svj_st<T, MT, GL>(a + sc * lda, gl, sw, sa);
+                    svj_st<T, NT, GL>(v + sc * ldv, gl, sw, sv);
+                    if (gl == 0) nrm[sc] = s_nrm;
                 }
                 __syncthreads();
             }
@@ -515,11 +548,11 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
         }
         if (converged || restarted || !budgeted) break;
         // warm budget spent: restart cold from A with V = I
-        for (int e = tid; e < MR * n; e += SVJ_CTA_THREADS) {
+        for (int e = tid; e < MR * n; e += THREADS) {
             const int i = e % MR, j = e / MR;
             a[j * lda + i] = i < m ? ag[(int64_t)j * m + i] : T(0);
         }
-        for (int e = tid; e < NR * n; e += SVJ_CTA_THREADS) {
+        for (int e = tid; e < NR * n; e += THREADS) {
             const int i = e % NR, j = e / NR;
             v[j * ldv + i] = (i == j) ? T(1) : T(0);
         }
@@ -529,7 +562,7 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
         }
         // ---- epilogue: normalise V; sigma_j = |A v_j| from the original A (see
         // the warp kernel); U from the rotated columns, normalised
-        for (int j = tid / 32; j < n; j += SVJ_CTA_THREADS / 32) {
+        for (int j = tid / 32; j < n; j += THREADS / 32) {
             T s2 = 0.f;
             for (int i = tid % 32; i < n; i += 32) s2 = fma(v[j * ldv + i], v[j * ldv + i], s2);
             s2 = warp_sum(s2);
@@ -537,7 +570,7 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
             for (int i = tid % 32; i < n; i += 32) v[j * ldv + i] *= inv;
         }
         __syncthreads();
-        for (int j = tid / 32; j < n; j += SVJ_CTA_THREADS / 32) {
+        for (int j = tid / 32; j < n; j += THREADS / 32) {
             T s2 = 0.f;
             for (int i = tid % 32; i < m; i += 32) {
                 T b = 0.f;
@@ -557,7 +590,7 @@ __global__ void __launch_bounds__(SVJ_CTA_THREADS, sizeof(T) == 8 ? 2 : 3)
         T smax = 0.f;
         for (int k = 0; k < n; k++) smax = fmax(smax, sig[k]);
         const T thr = smax * (T)(m > n ? m : n) * mach_eps<T>();
-        for (int j = tid; j < n; j += SVJ_CTA_THREADS) {
+        for (int j = tid; j < n; j += THREADS) {
             int ps = 0;
             for (int k = 0; k < n; k++) ps += (sig[k] > sig[j] || (sig[k] == sig[j] && k < j)) ? 1 : 0;
             const T inv_rot = rinv[j];
@@ -627,14 +660,14 @@ template <typename T, int MR, int NR>
 static gbla_status svj_cta_launch(int m, int n, const T *A, int64_t sA, T *S, int64_t sS, T *Vt, int64_t sVt, T *U,
                                   int64_t sU, const T *V0, int64_t sV0, T tol, int max_sweeps, int warm_budget,
                                   int *fallback, int *info, int *sweeps, int batch, size_t smem, cudaStream_t st) {
+    constexpr int threads = 32 * svj_group<T, MR>();
     if (smem > 48 * 1024) {
         cudaError_t e =
             cudaFuncSetAttribute(k_gesvj_cta<T, MR, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return from_cuda(e);
     }
-    const int64_t grid =
-        persistent_grid(reinterpret_cast<const void *>(k_gesvj_cta<T, MR, NR>), SVJ_CTA_THREADS, smem, batch);
-    k_gesvj_cta<T, MR, NR><<<(unsigned)grid, SVJ_CTA_THREADS, smem, st>>>(
+    const int64_t grid = persistent_grid(reinterpret_cast<const void *>(k_gesvj_cta<T, MR, NR>), threads, smem, batch);
+    k_gesvj_cta<T, MR, NR><<<(unsigned)grid, threads, smem, st>>>(
         m, n, A, sA, S, sS, Vt, sVt, U, sU, V0, sV0, tol, max_sweeps, warm_budget, fallback, info, sweeps, batch);
     return launch_status();
 }
