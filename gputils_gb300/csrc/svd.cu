@@ -59,6 +59,13 @@ template <> __device__ __forceinline__ float unit_roundoff<float>() { return 5.9
 template <> __device__ __forceinline__ double unit_roundoff<double>() { return 1.1102230246251565e-16; }
 template <typename T> __device__ __forceinline__ T mach_eps() { return T(2) * unit_roundoff<T>(); }
 
+// 2^e and the binary exponent of x > 0 (x = f 2^e, f in [1, 2)).
+template <typename T> __device__ __forceinline__ T pow2(int e);
+template <> __device__ __forceinline__ float pow2<float>(int e) { return ldexpf(1.0f, e); }
+template <> __device__ __forceinline__ double pow2<double>(int e) { return ldexp(1.0, e); }
+__device__ __forceinline__ int ilogb_of(float x) { return ilogbf(x); }
+__device__ __forceinline__ int ilogb_of(double x) { return ilogb(x); }
+
 // Tolerance actually used: the request, but not below the FP32 noise floor
 // of |a_p . a_q| / (|a_p| |a_q|) for m-row columns.
 template <typename T>
@@ -105,6 +112,31 @@ __device__ __forceinline__ bool jacobi_rotation_t<double>(double alpha, double b
     c = 1.0 / sqrt(fma(t, t, 1.0));
     s = c * t;
     return true;
+}
+
+// FP32 block kernel, columns scaled so that |A|_F^2 < 4 (no square below can
+// overflow): the threshold test as gamma^2 > tol^2 alpha beta, and with
+// d = beta - alpha, t = 2 gamma / (d + sign(d) sqrt(d^2 + 4 gamma^2)), the
+// same Rutishauser t (|t| <= 1) with one square root and one reciprocal in
+// the dependency chain.
+__device__ __forceinline__ bool jacobi_rotation_scaled(float alpha, float beta, float gamma, float tol, float small,
+                                                       float &c, float &s, float &t) {
+    if (alpha <= small || beta <= small || gamma == 0.0f) return false;
+    if (!(gamma * gamma > (tol * tol) * alpha * beta)) return false;
+    const float d = beta - alpha;
+    const float r = sqrtf(fmaf(d, d, 4.0f * gamma * gamma));
+    t = __fdividef(2.0f * gamma, d + copysignf(r, d));
+    if (t == 0.0f) return false;
+    const float x = fmaf(t, t, 1.0f);
+    float y = rsqrtf(x);
+    y = y * fmaf(-0.5f * x * y, y, 1.5f);
+    c = y;
+    s = c * t;
+    return true;
+}
+__device__ __forceinline__ bool jacobi_rotation_scaled(double alpha, double beta, double gamma, double tol,
+                                                       double small, double &c, double &s, double &t) {
+    return jacobi_rotation_t<double>(alpha, beta, gamma, tol, small, c, s, t);
 }
 
 // ----------------------------------------------------------- warp kernel
@@ -447,7 +479,13 @@ __global__ void __launch_bounds__(32 * GL, svj_min_blocks<T, MR>())
             if (tid == 0) sig[0] = f;
         }
         __syncthreads();
-        const T small = mach_eps<T>() * mach_eps<T>() * sig[0];
+        // power-of-two scale (exact) bringing |A|_F^2 to [1, 4), so that the
+        // squares in the rotation angle cannot overflow
+        const T fro2 = sig[0];
+        const T psc = (fro2 > T(0) && isfinite(fro2)) ? pow2<T>(-(ilogb_of(fro2) >> 1)) : T(1);
+        if (psc != T(1))
+            for (int e = tid; e < MR * n; e += THREADS) a[(e / MR) * lda + e % MR] *= psc;
+        const T small = mach_eps<T>() * mach_eps<T>() * (fro2 * psc * psc);
         const T tol_eff = jacobi_tol<T>(tol, m);
         __syncthreads();
         const bool budgeted = V0 && warm_budget > 0;
@@ -505,16 +543,20 @@ __global__ void __launch_bounds__(32 * GL, svj_min_blocks<T, MR>())
                     T xm[MT];
                     if (act) {
                         svj_ld<T, MT, GL>(am, gl, sw, xm);
+                        T g3 = T(0), g4 = T(0);
 #pragma unroll
-                        for (int t = 0; t < MT; t += 2) {
+                        for (int t = 0; t < MT; t += 4) {
                             gamma = fma(sa[t], xm[t], gamma);
                             g2 = fma(sa[t + 1], xm[t + 1], g2);
+                            g3 = fma(sa[t + 2], xm[t + 2], g3);
+                            g4 = fma(sa[t + 3], xm[t + 3], g4);
                         }
+                        gamma = (gamma + g2) + (g3 + g4);
                         beta = nrm[mc];
                     }
-                    gamma = group_sum(gamma + g2, GL);
+                    gamma = group_sum(gamma, GL);
                     T c, sn, tn;
-                    if (act && jacobi_rotation_t<T>(s_nrm, beta, gamma, tol_eff, small, c, sn, tn)) {
+                    if (act && jacobi_rotation_scaled(s_nrm, beta, gamma, tol_eff, small, c, sn, tn)) {
                         rotated = 1;
                         s_dirty = true;
 #pragma unroll
@@ -552,10 +594,10 @@ __global__ void __launch_bounds__(32 * GL, svj_min_blocks<T, MR>())
             if (!__syncthreads_or(rotated)) { converged = 1; break; }
         }
         if (converged || restarted || !budgeted) break;
-        // warm budget spent: restart cold from A with V = I
+        // warm budget spent: restart cold from A (same power-of-two scale) with V = I
         for (int e = tid; e < MR * n; e += THREADS) {
             const int i = e % MR, j = e / MR;
-            a[j * lda + i] = i < m ? ag[(int64_t)j * m + i] : T(0);
+            a[j * lda + i] = i < m ? ag[(int64_t)j * m + i] * psc : T(0);
         }
         for (int e = tid; e < NR * n; e += THREADS) {
             const int i = e % NR, j = e / NR;
