@@ -182,7 +182,12 @@ __global__ void __launch_bounds__(128, 1)
     T fro2 = 0.f;
 #pragma unroll
     for (int i = 0; i < MR; i++) fro2 = fma(a[i], a[i], fro2);
-    const T small = mach_eps<T>() * mach_eps<T>() * warp_sum(fro2);
+    fro2 = warp_sum(fro2);
+    // power-of-two scale (exact) bringing |A|_F^2 to [1, 4) (jacobi_rotation_scaled)
+    const T psc = (fro2 > T(0) && isfinite(fro2)) ? pow2<T>(-(ilogb_of(fro2) >> 1)) : T(1);
+#pragma unroll
+    for (int i = 0; i < MR; i++) a[i] *= psc;
+    const T small = mach_eps<T>() * mach_eps<T>() * (fro2 * psc * psc);
     tol = jacobi_tol<T>(tol, m);
 
     // warm start with a sweep budget: past it, restart cold from A (V = I)
@@ -225,7 +230,7 @@ __global__ void __launch_bounds__(128, 1)
             for (int i = 0; i < MR; i++) gamma = fma(low ? a[i] : o[i], low ? o[i] : a[i], gamma);
             T c = 1.f, s = 0.f, t = 0.f;
             const T ap = low ? own : beta_o, aq = low ? beta_o : own;
-            bool rot = active && jacobi_rotation_t<T>(ap, aq, gamma, tol, small, c, s, t);
+            bool rot = active && jacobi_rotation_scaled(ap, aq, gamma, tol, small, c, s, t);
             // a_p' = c a_p - s a_q ; a_q' = s a_p + c a_q
             const T cm = c, so = low ? -s : s;
             if (__any_sync(FULL, rot)) {  // V's partner column only when some pair of the warp rotates
@@ -248,7 +253,7 @@ __global__ void __launch_bounds__(128, 1)
     if (converged || restarted || !budgeted) break;
     if constexpr (BUDGET) {
 #pragma unroll
-        for (int i = 0; i < MR; i++) a[i] = (col && i < m) ? ag[(int64_t)lane * m + i] : 0.f;
+        for (int i = 0; i < MR; i++) a[i] = (col && i < m) ? ag[(int64_t)lane * m + i] * psc : 0.f;
 #pragma unroll
         for (int i = 0; i < 32; i++) v[i] = (col && i == lane) ? 1.f : 0.f;
         restarted = 1;
