@@ -426,18 +426,39 @@ __global__ void __launch_bounds__(WS_T)
 }
 
 // V0 for a batch, without forming the inverse: V0 = Vb (2 (I - S)^{-1} - I),
-// so V0^T = 2 (I + S)^{-1} Vb^T - Vb^T, and one Gauss-Jordan elimination of
-// [I + S | Vb^T] (64 x 128 in registers, the thread mapping of
-// sm_cayley_inverse; I + S also has symmetric part I, so no pivoting) leaves
-// Y = (I + S)^{-1} Vb^T in the right half.  Thread (row r, column c of Y)
+// so V0^T = 2 (I + S)^{-1} Vb^T - Vb^T: a Gauss-Jordan elimination of
+// [I + S | Vb^T] (64 x 128 in registers; I + S has symmetric part I, so no
+// pivoting) leaves D Y in the right half, D the diagonal the left half ends
+// as and Y = (I + S)^{-1} Vb^T.  Thread t holds rows 4 (t >> 4) + a and
+// columns 8 (t & 15) + q, so warp w holds rows 8w .. 8w + 7 across all 128
+// columns.  The elimination runs in eight blocks of eight pivots: warp b
+// eliminates within its own rows (pivot row and column by shuffle, no block
+// barrier), publishes its rows and every row's entries in its pivot columns,
+// and after one block barrier every other warp applies the rank-8 update
+// (row i loses sum_p (m_{i,8b+p} / d_p) R_p: the block's rows R_p are zero in
+// each other's pivot columns).  Pivot rows are never scaled; D is divided
+// out at the end.  The network outputs are staged through shared memory so
+// that their global reads are coalesced.  Thread (row r, column c of Y)
 // writes V0[r n + c] = V0(c, r) = 2 Y(r, c) - Vb(c, r), contiguous in c.
+struct FrameBuf {
+    float o[64 * 63 / 2];    // the network outputs of the matrix (strict upper triangle of S)
+    float prow[2][8][128];   // the pivot block's rows, double-buffered by block parity
+    float pcol[2][64][8];    // every row's entries in the block's pivot columns
+    float dinv[64];          // 1 / d_k
+};
+
 __global__ void __launch_bounds__(WS_T, 3)
     k_ws_frame(int n, int P, const float *__restrict__ out, const float *__restrict__ Vbase, float *__restrict__ V0g,
                int64_t sV0, int batch) {
-    __shared__ GJBuf gb;
-    const int t = threadIdx.x, r0 = (t & 15) * 4, c0 = (t >> 4) * 8;
+    __shared__ __align__(16) FrameBuf fb;
+    const int t = threadIdx.x, rg = t >> 4, cg = t & 15, r0 = 4 * rg, c0 = 8 * cg;
+    const int warp = t >> 5, lane = t & 31;
+    const int nblk = (n + 7) >> 3;
     for (int b = blockIdx.x; b < batch; b += gridDim.x) {
         const float *o = out + (int64_t)b * P;
+        __syncthreads();  // the previous matrix is done with the buffers
+        for (int e = t; e < P; e += WS_T) fb.o[e] = o[e];
+        __syncthreads();
         float m[4][8];
 #pragma unroll
         for (int a = 0; a < 4; a++)
@@ -447,59 +468,83 @@ __global__ void __launch_bounds__(WS_T, 3)
                 float v;
                 if (c < 64) {
                     v = r == c ? 1.0f : 0.0f;
-                    if (r < n && c < n && r != c) v = r < c ? o[upper_index(r, c, n)] : -o[upper_index(c, r, n)];
+                    if (r < n && c < n && r != c) v = r < c ? fb.o[upper_index(r, c, n)] : -fb.o[upper_index(c, r, n)];
                 } else {
                     // Vb^T(r, c - 64) = Vb(c - 64, r), column-major Vb
                     v = (r < n && c - 64 < n) ? Vbase[r * n + (c - 64)] : 0.0f;
                 }
                 m[a][q] = v;
             }
-        for (int kk = 0; kk < n; kk += 8) {
+        for (int blk = 0; blk < nblk; blk++) {
+            const int par = blk & 1;
+            if (warp == blk) {
+                // eliminate within rows 8 blk .. 8 blk + 7: pivot k = 8 blk + p sits in
+                // lane 16 (p >> 2) + cg (row slot p & 3), its column in column group blk
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const int k = kk + q;
-                if (k >= n) break;
-                const int par = k & 1;
-                if (c0 == kk) {
+                for (int p = 0; p < 8; p++) {
+                    const int src_row = 16 * (p >> 2);
+                    float pr[8];
 #pragma unroll
-                    for (int a = 0; a < 4; a++) gb.pcol[par][r0 + a] = m[a][q];
-                }
-                __syncthreads();
-                if (r0 == (k & ~3)) {
-                    const float inv = 1.0f / gb.pcol[par][k];
+                    for (int q = 0; q < 8; q++) pr[q] = shfl(m[p & 3][q], src_row + cg);
+                    const float piv = shfl(m[p & 3][p], src_row + blk);
+                    float f[4];
 #pragma unroll
-                    for (int qq = 0; qq < 8; qq++) {
-                        m[q & 3][qq] *= inv;
-                        gb.prow[par][c0 + qq] = m[q & 3][qq];
+                    for (int a = 0; a < 4; a++) f[a] = shfl(m[a][p], (lane & 16) + blk);
+                    const float ip = 1.0f / piv;
+#pragma unroll
+                    for (int a = 0; a < 4; a++) {
+                        if ((lane >> 4) == (p >> 2) && a == (p & 3)) continue;  // the pivot row itself
+                        const float fa = f[a] * ip;
+#pragma unroll
+                        for (int q = 0; q < 8; q++) m[a][q] = fmaf(-fa, pr[q], m[a][q]);
                     }
+                    if (lane == 0) fb.dinv[8 * blk + p] = ip;
                 }
-                __syncthreads();
-                float pr[8];
 #pragma unroll
-                for (int qq = 0; qq < 8; qq++) pr[qq] = gb.prow[par][c0 + qq];
+                for (int a = 0; a < 4; a++)
 #pragma unroll
-                for (int a = 0; a < 4; a++) {
-                    if (r0 + a == k) continue;
-                    const float f = gb.pcol[par][r0 + a];
+                    for (int q = 0; q < 8; q++) fb.prow[par][4 * (lane >> 4) + a][c0 + q] = m[a][q];
+            }
+            if (cg == blk && warp != blk) {
 #pragma unroll
-                    for (int qq = 0; qq < 8; qq++) m[a][qq] = fmaf(-f, pr[qq], m[a][qq]);
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int q = 0; q < 8; q++) fb.pcol[par][r0 + a][q] = m[a][q];
+            }
+            __syncthreads();
+            if (warp != blk) {
+                float di[8];
+#pragma unroll
+                for (int p = 0; p < 8; p++) di[p] = fb.dinv[8 * blk + p];
+#pragma unroll
+                for (int p = 0; p < 8; p++) {
+                    float pr[8];
+#pragma unroll
+                    for (int q = 0; q < 8; q++) pr[q] = fb.prow[par][p][c0 + q];
+#pragma unroll
+                    for (int a = 0; a < 4; a++) {
+                        const float fa = fb.pcol[par][r0 + a][p] * di[p];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) m[a][q] = fmaf(-fa, pr[q], m[a][q]);
+                    }
                 }
             }
         }
+        __syncthreads();  // every 1 / d_k is published
         if (c0 >= 64) {
             float *dst = V0g + (int64_t)b * sV0;
 #pragma unroll
             for (int a = 0; a < 4; a++) {
                 const int r = r0 + a;
                 if (r >= n) continue;
+                const float inv = fb.dinv[r];
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
                     const int c = c0 - 64 + q;
-                    if (c < n) dst[r * n + c] = 2.0f * m[a][q] - Vbase[r * n + c];
+                    if (c < n) dst[r * n + c] = 2.0f * (m[a][q] * inv) - Vbase[r * n + c];
                 }
             }
         }
-        __syncthreads();
     }
 }
 
