@@ -68,6 +68,30 @@ __device__ __forceinline__ T reduce_scatter32(T (&p)[32], int lane) {
     return mine + shfl_xor(other, 1);
 }
 
+// Householder coefficients of a column with leading entry alpha and squared
+// norm x2 > 0 below it (LAPACK dlarfg convention): beta = -sign(alpha)
+// sqrt(alpha^2 + x2), tau = (beta - alpha) / beta, scal = 1 / (alpha - beta).
+// FP32: from one Newton-refined reciprocal square root y = 1 / sqrt(alpha^2 +
+// x2) (about 1 ulp) -- beta = -sign(alpha) s y, tau = 1 + |alpha| y, scal =
+// sign(alpha) / (|alpha| + s y) -- a shorter dependency chain than a square
+// root and two divisions on the critical path of every step.  FP64: as LAPACK.
+template <typename T>
+__device__ __forceinline__ void house_coeffs(T alpha, T x2, T &beta, T &tau, T &scal) {
+    if constexpr (sizeof(T) == 4) {
+        const float s2 = fmaf(alpha, alpha, x2);
+        float y = rsqrtf(s2);
+        y = y * fmaf(-0.5f * s2 * y, y, 1.5f);
+        const float r = s2 * y;  // sqrt(alpha^2 + x2)
+        beta = -copysignf(r, alpha);
+        tau = fmaf(fabsf(alpha), y, 1.0f);
+        scal = copysignf(__fdividef(1.0f, fabsf(alpha) + r), alpha);
+    } else {
+        beta = -copysign(dev_sqrt<T>(fma(alpha, alpha, x2)), alpha);
+        tau = (beta - alpha) / beta;
+        scal = T(1) / (alpha - beta);
+    }
+}
+
 // --------------------------------------------------------- warp QR core
 template <typename T, int R>
 struct QrWarp {
@@ -93,10 +117,9 @@ struct QrWarp {
                 T tau = T(0);
                 if (lane == k) rdiag = alpha;
                 if (x2 > T(0)) {
-                    const T beta = -copysign(dev_sqrt<T>(fma(alpha, alpha, x2)), alpha);
+                    T beta, scal;
+                    house_coeffs<T>(alpha, x2, beta, tau, scal);
                     if (lane == k) rdiag = beta;
-                    tau = (beta - alpha) / beta;
-                    const T scal = T(1) / (alpha - beta);
 #pragma unroll
                     for (int t = 0; t < R; t++)
                         if (row(t) > k) a[t][k] *= scal;
@@ -594,9 +617,8 @@ __global__ void __launch_bounds__(128)
                 const float alpha = shfl(a[0][kb], k);
                 float tau = 0.f;
                 if (x2 > 0.f) {
-                    const float beta = -copysignf(sqrtf(fmaf(alpha, alpha, x2)), alpha);
-                    tau = (beta - alpha) / beta;
-                    const float scal = 1.f / (alpha - beta);
+                    float beta, scal;
+                    house_coeffs<float>(alpha, x2, beta, tau, scal);
 #pragma unroll
                     for (int t = 0; t < R; t++)
                         if (lane + 32 * t > k) a[t][kb] *= scal;
