@@ -12,6 +12,9 @@
 //   refp_spotrf_batched cusolverDnSpotrfBatched(LOWER)                      tensor.cuh:2149-2159
 //   refp_spotrs_batched cusolverDnSpotrsBatched(LOWER, nrhs = 1)            tensor.cuh:2180-2197
 //   refp_sgesvd_loop    host loop of cusolverDnSgesvd('A'|'N', 'A')          tensor.cuh:1651-1676
+//   refp_spotrf         CholeskyFactoriser<float>: workspace sized once
+//                       (cusolverDnSpotrf_bufferSize), factorise = cusolverDnSpotrf(LOWER)
+//                                                                            tensor.cuh:1703-1709, 1735-1740, 1754-1761
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
@@ -52,6 +55,14 @@ REFP_API int refp_spotrf_batched(int n, float **A, int *info, int batch) {
 
 REFP_API int refp_spotrs_batched(int n, float **A, float **B, int *info, int batch) {
     return (int)cusolverDnSpotrsBatched(g_solver, CUBLAS_FILL_MODE_LOWER, n, 1, A, n, B, n, info, batch);
+}
+
+REFP_API int refp_spotrf_bufsize(int n, int *lwork) {
+    return (int)cusolverDnSpotrf_bufferSize(g_solver, CUBLAS_FILL_MODE_LOWER, n, nullptr, n, lwork);
+}
+
+REFP_API int refp_spotrf(int n, float *A, float *work, int lwork, int *info) {
+    return (int)cusolverDnSpotrf(g_solver, CUBLAS_FILL_MODE_LOWER, n, A, n, work, lwork, info);
 }
 
 REFP_API int refp_dpotrf_batched(int n, double **A, int *info, int batch) {

@@ -20,6 +20,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include "common.cuh"
+#include "gemm_bf16.cuh"
 
 namespace gbla {
 
@@ -32,6 +33,7 @@ constexpr uint32_t BG_TMEM_COLS = 128;
 constexpr uint32_t BG_SPIN_LIMIT = 1u << 26;
 
 __device__ int g_bf16_gemm_error = 0;
+
 
 namespace {
 
@@ -93,7 +95,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 
 __global__ void __launch_bounds__(BG_THREADS, 2)
     k_gemm_bf16_tn(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int M, int N,
-                   int K, const gbla_bf16_epilogue epi) {
+                   int K, const gbla_bf16_epilogue epi, const Bf16EpiX ex) {
     extern __shared__ unsigned char bg_raw[];
     // 1024-byte alignment for the 128-byte swizzle pattern
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(bg_raw) + 1023) & ~uintptr_t(1023));
@@ -107,6 +109,7 @@ __global__ void __launch_bounds__(BG_THREADS, 2)
     // read it once from DRAM (through L2)
     const int m0 = blockIdx.y * BG_BM, n0 = blockIdx.x * BG_BN;
     const int KT = (K + BG_BK - 1) / BG_BK;
+    if (ex.lower && n0 + BG_BN <= m0) return;  // every element of the tile has n < m (whole CTA, before any setup)
 
     if (tid == 0) {
         for (int s = 0; s < BG_STAGES; s++) {
@@ -202,15 +205,25 @@ __global__ void __launch_bounds__(BG_THREADS, 2)
                     x[e] = t;
                 }
                 const bool whole = nb + 32 <= N;
-                if (epi.out_f32) {
+                if (epi.out_f32 && !(ex.lower && nb + 32 <= m)) {
                     float *dst = epi.out_f32 + (int64_t)m * epi.ld_f32 + nb;
-                    if (whole && ((uintptr_t)dst & 15) == 0) {
+                    if (whole && (!ex.lower || nb >= m) && ((uintptr_t)dst & 15) == 0) {
 #pragma unroll
-                        for (int e = 0; e < 32; e += 4)
-                            *reinterpret_cast<float4 *>(dst + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
+                        for (int e = 0; e < 32; e += 4) {
+                            float4 o = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
+                            if (ex.beta != 0.0f) {
+                                const float4 c = *reinterpret_cast<const float4 *>(dst + e);
+                                o.x = fmaf(ex.beta, c.x, o.x);
+                                o.y = fmaf(ex.beta, c.y, o.y);
+                                o.z = fmaf(ex.beta, c.z, o.z);
+                                o.w = fmaf(ex.beta, c.w, o.w);
+                            }
+                            *reinterpret_cast<float4 *>(dst + e) = o;
+                        }
                     } else {
                         for (int e = 0; e < 32; e++)
-                            if (nb + e < N) dst[e] = x[e];
+                            if (nb + e < N && (!ex.lower || nb + e >= m))
+                                dst[e] = ex.beta != 0.0f ? fmaf(ex.beta, dst[e], x[e]) : x[e];
                     }
                 }
                 if (epi.out_bf16) {
@@ -299,8 +312,8 @@ bool make_map(CUtensorMap *map, const void *base, int64_t rows, int64_t cols, in
 
 }  // namespace
 
-gbla_status gemm_bf16_tn(int M, int N, int K, const void *A, int64_t lda, const void *B, int64_t ldb,
-                         const gbla_bf16_epilogue &epi, cudaStream_t st) {
+gbla_status gemm_bf16_tn_ex(int M, int N, int K, const void *A, int64_t lda, const void *B, int64_t ldb,
+                            const gbla_bf16_epilogue &epi, const Bf16EpiX &ex, cudaStream_t st) {
     if (M < 0 || N < 0 || K < 0) return GBLA_INVALID_VALUE;
     if (M == 0 || N == 0) return GBLA_SUCCESS;
     if (!A || !B || K == 0) return GBLA_INVALID_VALUE;
@@ -323,8 +336,13 @@ gbla_status gemm_bf16_tn(int M, int N, int K, const void *A, int64_t lda, const 
     }
     dim3 grid((unsigned)((N + BG_BN - 1) / BG_BN), (unsigned)((M + BG_BM - 1) / BG_BM));
     if (grid.y > 65535) return GBLA_INVALID_VALUE;
-    k_gemm_bf16_tn<<<grid, BG_THREADS, BG_SMEM, st>>>(ma, mb, M, N, K, epi);
+    k_gemm_bf16_tn<<<grid, BG_THREADS, BG_SMEM, st>>>(ma, mb, M, N, K, epi, ex);
     return launch_status();
+}
+
+gbla_status gemm_bf16_tn(int M, int N, int K, const void *A, int64_t lda, const void *B, int64_t ldb,
+                         const gbla_bf16_epilogue &epi, cudaStream_t st) {
+    return gemm_bf16_tn_ex(M, N, K, A, lda, B, ldb, epi, Bf16EpiX{0.0f, 0}, st);
 }
 
 }  // namespace gbla

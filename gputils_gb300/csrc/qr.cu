@@ -23,11 +23,10 @@ static gbla_status gels_ws_launch(int m, int n, int nrhs, float *A, int64_t sA, 
     float *tau = F + (size_t)batch * m * n;
     const int R = (m + 31) / 32;
     const unsigned g1 = (unsigned)((batch + 3) / 4);
-    const size_t smem1 = (size_t)4 * 32 * sizeof(float);
     const size_t smem2 = sizeof(float) * ((size_t)32 * (32 * R + 1) + (refine > 0 ? 32 * 32 * R : 0) + 32);
     auto go = [&](auto kf, auto ks) -> gbla_status {
-        kf<<<g1, 128, smem1, st>>>(m, n, 0, A, sA, nullptr, 0, tau, 32, info, QR_WRITE_FACTORS | QR_WRITE_TAU, 0,
-                                   batch, F, (int64_t)m * n);
+        kf<<<g1, 128, 0, st>>>(m, n, 0, A, sA, nullptr, 0, tau, 32, info, QR_WRITE_FACTORS | QR_WRITE_TAU, batch, F,
+                               (int64_t)m * n);
         gbla_status s = launch_status();
         if (s != GBLA_SUCCESS) return s;
         if (smem2 > 48 * 1024) {

@@ -319,18 +319,11 @@ __device__ __forceinline__ float refine_ls(const QF &q, const float *A0, int lda
 template <typename T, int R, bool SOLVE = true>
 __global__ void __launch_bounds__(128, (SOLVE || sizeof(T) == 8) ? 1 : 3)
     k_qr_warp(int m, int n, int nrhs, T *__restrict__ A, int64_t sA, T *__restrict__ B, int64_t sB,
-              T *__restrict__ tau_g, int64_t sTau, int *__restrict__ info, int flags, int refine, int batch,
+              T *__restrict__ tau_g, int64_t sTau, int *__restrict__ info, int flags, int batch,
               T *__restrict__ F = nullptr, int64_t sF = 0) {
-    extern __shared__ __align__(16) unsigned char qsm_raw[];
-    T *qsm = reinterpret_cast<T *>(qsm_raw);
+    __shared__ T tau_all[4 * 32];  // 32 taus per warp
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int LDM = 32 * R;
-    constexpr bool kRefinable = sizeof(T) == 4;  // double needs no extended precision
-    if (!kRefinable) refine = 0;
-    // per warp: [original A, LDM x 32, only when refining] [32 taus]
-    const int a0_elems = refine > 0 ? LDM * 32 : 0;
-    T *A0 = qsm + warp * (a0_elems + 32);
-    T *tau_s = A0 + a0_elems;
+    T *tau_s = tau_all + 32 * warp;
     const int64_t mat = (int64_t)blockIdx.x * 4 + warp;
     if (mat >= batch) return;  // whole warp leaves together; no block barriers below
     QrWarp<T, R> q;
@@ -343,7 +336,6 @@ __global__ void __launch_bounds__(128, (SOLVE || sizeof(T) == 8) ? 1 : 3)
             int r = lane + 32 * t;
             T v = (j < n && r < m) ? a_g[(int64_t)j * m + r] : T(0);
             q.a[t][j] = v;
-            if (refine > 0) A0[j * LDM + r] = v;
         }
     int fail = q.factor(m, n, tau_s);
     if (info && lane == 0) info[mat] = fail;
@@ -351,18 +343,14 @@ __global__ void __launch_bounds__(128, (SOLVE || sizeof(T) == 8) ? 1 : 3)
     if (SOLVE && (flags & QR_SOLVE) && nrhs > 0) {
         T *b_g = B + mat * sB;
         for (int c = 0; c < nrhs; c++) {
-            T y[R], b[R];
+            T y[R];
 #pragma unroll
             for (int t = 0; t < R; t++) {
                 int r = lane + 32 * t;
-                b[t] = r < m ? b_g[(int64_t)c * m + r] : T(0);
-                y[t] = b[t];
+                y[t] = r < m ? b_g[(int64_t)c * m + r] : T(0);
             }
             q.apply_qt(n, tau_s, y);
-            T x = q.back_solve(n, lane < n ? y[0] : T(0));
-            if constexpr (kRefinable) {
-                if (refine > 0) x = refine_ls<R>(q, A0, LDM, m, n, b, x, tau_s, refine);
-            }
+            const T x = q.back_solve(n, lane < n ? y[0] : T(0));
             // rows < n: solution (row r = this lane when t = 0, since n <= 32);
             // rows >= n: (Q^T b)(n:m), as gels leaves them
 #pragma unroll
@@ -752,16 +740,9 @@ static inline gbla_status qr_launch(int m, int n, int nrhs, T *A, int64_t sA, T 
     if (sizeof(T) != 4) refine = 0;
     if (m > 128 || n > 32) return qr_big_launch<T>(m, n, nrhs, A, sA, B, sB, tau, sTau, info, flags, refine, batch, st);
     const int R = (m + 31) / 32;
-    // shared memory: per warp the original A (refinement only) and 32 taus
-    size_t smem = (size_t)4 * ((refine > 0 ? 32 * R * 32 : 0) + 32) * sizeof(T);
     const unsigned grid = (unsigned)((batch + 3) / 4);
     auto go = [&](auto kern) -> gbla_status {
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return from_cuda(e);
-        }
-        kern<<<grid, 128, smem, st>>>(m, n, nrhs, A, sA, B, sB, tau, sTau, info, flags, refine, batch,
-                                      (T *)nullptr, (int64_t)0);
+        kern<<<grid, 128, 0, st>>>(m, n, nrhs, A, sA, B, sB, tau, sTau, info, flags, batch, (T *)nullptr, (int64_t)0);
         return launch_status();
     };
     if constexpr (sizeof(T) == 8) {

@@ -88,6 +88,21 @@ gbla_status gbla_spotrf_batched(int n, float *A, int64_t strideA, int *info, int
 gbla_status gbla_dpotrf_batched(int n, double *A, int64_t strideA, int *info, int batch,
                                 cudaStream_t stream);
 
+/* In-place lower Cholesky of ONE large n x n FP32 matrix (column stride
+ * lda >= n) on the whole GPU: right-looking blocked factorisation with
+ * 128-column panels -- the diagonal block by one thread block, the panel
+ * below it by n / 64 blocks, and the trailing update A22 -= L21 L21^T on the
+ * tensor cores (tcgen05; L21 split exactly into three BF16 parts, the six
+ * largest of the nine products accumulated in FP32).  The strictly upper
+ * triangle is not touched; *info as gbla_spotrf_batched (set to 0 first).
+ * Any n >= 0; the workspace (gbla_spotrf_large_workspace_bytes, 3 KB per
+ * row, none for n <= 128) holds the BF16 operands.  Replaces cusolverDnSpotrf
+ * (include/tensor.cuh:1742-1761: CholeskyFactoriser::factorise) for the sizes
+ * where gbla_spotrf_batched with batch = 1 would leave all but one SM idle. */
+size_t gbla_spotrf_large_workspace_bytes(int n);
+gbla_status gbla_spotrf_large(int n, float *A, int64_t lda, int *info, void *workspace,
+                              size_t workspace_bytes, cudaStream_t stream);
+
 /* Solve L_i L_i^T X_i = B_i in place (B_i is n x nrhs) with the lower factor
  * in L_i.  Replaces cusolverDn<t>potrsBatched (include/tensor.cuh:2161-2197)
  * and cusolverDn<t>potrs (include/tensor.cuh:1763-1783); nrhs >= 1 (the

@@ -25,6 +25,10 @@
  *    without it, like cuBLAS.
  *  - operator= releases what the target owned before aliasing the source.
  *  - Givens bounds are checked on every index, as the reference documents.
+ *  - CholeskyFactoriser<float> above n = 128 runs a blocked factorisation on
+ *    the whole GPU (trailing updates on the tensor cores, BF16x3 split with
+ *    FP32 accumulation); its workspace is sized and owned by the factoriser
+ *    as the reference's cuSOLVER workspace is.
  *  - Extensions with no reference counterpart: batched Givens rotations
  *    (DTensor::applyLeft/RightGivensRotationBatched, GivensAnnihilatorBatched),
  *    which rotate every matrix of a tensor in one launch.
@@ -273,6 +277,16 @@ inline gbla_status potrf(int n, float *A, int *info, int batch, cudaStream_t st)
 }
 inline gbla_status potrf(int n, double *A, int *info, int batch, cudaStream_t st) {
     return gbla_dpotrf_batched(n, A, (int64_t)n * n, info, batch, st);
+}
+// one large matrix on the whole GPU (float; n > 128): workspace bytes, then the call
+inline size_t potrf_large_ws(float *, int n) { return n > 128 ? gbla_spotrf_large_workspace_bytes(n) : 0; }
+inline size_t potrf_large_ws(double *, int) { return 0; }
+inline gbla_status potrf_one(int n, float *A, int *info, void *ws, size_t ws_bytes, cudaStream_t st) {
+    if (n > 128) return gbla_spotrf_large(n, A, n, info, ws, ws_bytes, st);
+    return gbla_spotrf_batched(n, A, (int64_t)n * n, info, 1, st);
+}
+inline gbla_status potrf_one(int n, double *A, int *info, void *, size_t, cudaStream_t st) {
+    return gbla_dpotrf_batched(n, A, (int64_t)n * n, info, 1, st);
 }
 inline gbla_status potrs(int n, int nrhs, const float *L, float *B, int batch, cudaStream_t st) {
     return gbla_spotrs_batched(n, nrhs, L, (int64_t)n * n, B, (int64_t)n * nrhs, batch, st);
@@ -943,17 +957,24 @@ TEMPLATE_CONSTRAINT_REQUIRES_FPX
 class CholeskyFactoriser : public IStatus {
 private:
     DTensor<T> *m_matrix;
+    std::unique_ptr<DTensor<float>> m_workspace;  // BF16 operands of the blocked float path (n > 128)
+    size_t m_workspaceBytes = 0;
 
 public:
     CholeskyFactoriser(DTensor<T> &A) : IStatus() {
         if (A.numMats() > 1) throw std::invalid_argument("[Cholesky] 3D tensors require `CholeskyBatchFactoriser`");
         if (A.numRows() != A.numCols()) throw std::invalid_argument("[Cholesky] Matrix A must be square");
         m_matrix = &A;
+        // as the reference sizes its cuSOLVER workspace here: float matrices
+        // above 128 are factored by the blocked whole-GPU path
+        m_workspaceBytes = gputils_detail::potrf_large_ws(m_matrix->raw(), (int)A.numRows());
+        if (m_workspaceBytes) m_workspace = std::make_unique<DTensor<float>>((m_workspaceBytes + 3) / 4);
     }
 
     void factorise() {
-        gputils_detail::check(gputils_detail::potrf((int)m_matrix->numRows(), m_matrix->raw(), m_info->raw(), 1,
-                                                    Session::getInstance().stream(m_matrix->streamIdx())),
+        gputils_detail::check(gputils_detail::potrf_one((int)m_matrix->numRows(), m_matrix->raw(), m_info->raw(),
+                                                        m_workspace ? m_workspace->raw() : nullptr, m_workspaceBytes,
+                                                        Session::getInstance().stream(m_matrix->streamIdx())),
                               "Cholesky");
     }
 

@@ -697,6 +697,42 @@ template <typename T> static void choleskyBig(size_t n, T eps) {
 }
 TEST(choleskyBatchBeyond128) { choleskyBig<float>(200, 1e-4f); choleskyBig<double>(300, 1e-11); }
 
+// CholeskyFactoriser on one large matrix (float: the blocked whole-GPU path
+// with tensor-core trailing updates; double: one thread block): factorise,
+// solve, residual of the solution against the original A.
+template <typename T>
+void choleskyLarge(size_t n, T eps) {
+    std::vector<T> g = randomVec<T>(n * n, 61), a(n * n, T(0));
+    for (size_t c = 0; c < n; c++)
+        for (size_t r = 0; r < n; r++) {
+            double acc = r == c ? 0.5 : 0.0;
+            for (size_t l = 0; l < n; l++) acc += (double)g[r * n + l] * g[c * n + l] / n;
+            a[c * n + r] = (T)acc;
+        }
+    DTensor<T> A(a, n, n, 1), b(randomVec<T>(n, 62), n, 1, 1), b0 = b;
+    CholeskyFactoriser<T> chol(A);
+    chol.factorise();
+    EXPECT_EQ(chol.info()(0), 0);
+    chol.solve(b);
+    std::vector<T> x, bb, l;
+    b.download(x);
+    b0.download(bb);
+    A.download(l);
+    double num = 0, den = 0;
+    for (size_t r = 0; r < n; r++) {
+        double acc = 0;
+        for (size_t c = 0; c < n; c++) acc += (double)a[c * n + r] * x[c];
+        num += (acc - bb[r]) * (acc - bb[r]);
+        den += (double)bb[r] * bb[r];
+    }
+    EXPECT_LT(std::sqrt(num / den), eps);
+    bool upper_kept = true;  // the strict upper triangle is not written
+    for (size_t c = 1; c < n; c++)
+        for (size_t r = 0; r < c; r++) upper_kept = upper_kept && l[c * n + r] == a[c * n + r];
+    EXPECT_TRUE(upper_kept);
+}
+TEST(choleskyFactoriserLarge) { choleskyLarge<float>(700, 1e-4f); choleskyLarge<double>(300, 1e-11); }
+
 // GivensAnnihilatorBatched zeroes (k, j) of every matrix with its own rotation;
 // applyLeftGivensRotationBatched with those coefficients reproduces it
 template <typename T> static void givensBatched(T eps) {
