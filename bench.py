@@ -66,7 +66,8 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["d2", "d1", "d3", "d4", "d5"], default="d2")
+    ap.add_argument("--workload", choices=["d2", "d1", "d3", "d4", "d5", "large"], default="d2",
+                    help="large: one --large-n matrix through CholeskyFactoriser<float> (part of the d2 line's workloads)")
     ap.add_argument("--dtype", choices=["f32", "f64"], default="f32", help="data type of the ragged workload d3")
     ap.add_argument("--ref-sample", type=int, default=0,
                     help="matrices the reference SVD host loop runs on (d4/d5; scaled to the batch)")
@@ -84,6 +85,7 @@ def parse_args(argv=None):
                     help="d3: threads,systems_per_block of the plan instead of autotuning (e.g. 768,8)")
     ap.add_argument("--ws-pairs", type=int, default=200_000, help="d5: (A, V) training pairs of the warm-start net")
     ap.add_argument("--ws-epochs", type=int, default=20, help="d5: training epochs of the warm-start net")
+    ap.add_argument("--large-n", type=int, default=4096, help="order of the one-matrix Cholesky in the workloads")
     return ap.parse_args(argv)
 
 
@@ -312,6 +314,10 @@ def run_reference_arm(args):
         if rank != 0:
             dist.barrier()
             return
+    if args.workload not in CPU_BASELINES:
+        print(json.dumps({"impl": "reference", "unavailable": f"no CPU sample for workload {args.workload}; its "
+                          "reference is the cuSOLVER call on the GPU, reported in our line"}), flush=True)
+        return
     # each step is a bounded sample: about cpu_seconds, and the whole run a few minutes at most
     budget = max(0.5, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
     fn = CPU_BASELINES[args.workload]
@@ -400,6 +406,8 @@ class RefLib:
         self.L.refp_dpotrs_batched.argtypes = [ip, vp, vp, vp, ip]
         self.L.refp_sgesvd_lwork.argtypes = [ip, ip]
         self.L.refp_sgesvd_loop.argtypes = [ip, ip, vp, vp, vp, vp, vp, ip, vp, ip, ip]
+        self.L.refp_spotrf_bufsize.argtypes = [ip, vp]
+        self.L.refp_spotrf.argtypes = [ip, vp, vp, ip, vp]
         assert self.L.refp_init(stream) == 0
 
 
@@ -1213,6 +1221,86 @@ def run_ours_d1(args, dev, st, L, rank, world, dist):
     }
 
 
+def run_chol_large(args, dev, st, L):
+    """CholeskyFactoriser<float>::factorise on one large SPD matrix (n = 4096,
+    M = G^T G / n + 0.5 I): the blocked whole-GPU path (diagonal blocks on one
+    CTA, panel solves on n/64 CTAs, trailing updates on the tensor cores)
+    against the reference's cusolverDnSpotrf on the same GPU and input.  The
+    factors are checked in FP64 on the GPU: ||L L^T - A|| / ||A||."""
+    import torch
+
+    n = args.large_n
+    g = torch.Generator(device=dev).manual_seed(4096)
+    G = torch.randn(n, n, device=dev, generator=g, dtype=torch.float64) / n ** 0.5
+    A64 = G.T @ G + 0.5 * torch.eye(n, device=dev, dtype=torch.float64)
+    A0 = A64.float().contiguous()  # symmetric: the same storage in either order
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    ws = torch.empty(max(1, L.gbla_spotrf_large_workspace_bytes(n)), dtype=torch.uint8, device=dev)
+    reps = max(3, min(args.steps, 5))
+
+    def timed(call):
+        A = A0.clone()
+        ts = []
+        for rep in range(2 + reps):
+            A.copy_(A0)
+            torch.cuda.synchronize()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record()
+            call(A)
+            e[1].record()
+            torch.cuda.synchronize()
+            if rep >= 2:
+                ts.append(e[0].elapsed_time(e[1]))
+        return float(np.median(ts)), A
+
+    def resid(A):
+        Lf = torch.tril(A.T.double())  # column-major storage read row-major is the transpose
+        return float(torch.linalg.matrix_norm(Lf @ Lf.T - A64) / torch.linalg.matrix_norm(A64))
+
+    ms, A = timed(lambda A: _lib_check(L.gbla_spotrf_large(n, A.data_ptr(), n, info.data_ptr(), ws.data_ptr(),
+                                                           ws.numel(), st), "spotrf_large"))
+    out = {"config": {"workload": f"CholeskyFactoriser<float>::factorise, one {n}x{n} SPD matrix (G^T G / n + 0.5 I)",
+                      "n": n},
+           "value": 1e3 / ms, "unit": "matrices/s", "ms": ms, "tflops": n ** 3 / 3 / ms / 1e9,
+           "info": int(info.item()), "max_rel_err_vs_fp64": {"LLt_minus_A": resid(A)},
+           # per call: a diagonal block per panel, a solve and a partial update for every panel but the last,
+           # and a side-stream update while more than 128 columns remain past the panel
+           "gpu_launches": (n + 127) // 128 + 2 * ((n + 127) // 128 - 1) + max(0, -(-(n - 256) // 128)),
+           "kernels": "k_potrf_diag + k_trsm_panel + k_gemm_bf16_tn (tcgen05, two per panel: next panel's columns "
+                      "and the rest, look-ahead on a side stream)"}
+    if not args.no_reference_library:
+        try:
+            R = RefLib(st)
+            lw = C.c_int(0)
+            assert R.L.refp_spotrf_bufsize(n, C.addressof(lw)) == 0
+            work = torch.empty(max(1, lw.value), dtype=torch.float32, device=dev)
+            rinfo = torch.zeros(1, dtype=torch.int32, device=dev)
+            rms, Ar = timed(lambda A: R.L.refp_spotrf(n, C.c_void_p(A.data_ptr()), C.c_void_p(work.data_ptr()),
+                                                      lw.value, C.c_void_p(rinfo.data_ptr())))
+            lo, lr = torch.tril(A.T.double()), torch.tril(Ar.T.double())
+            out["reference_library"] = {
+                "value": 1e3 / rms, "unit": "matrices/s", "ms": rms, "info": int(rinfo.item()),
+                "max_rel_err_vs_fp64": {"LLt_minus_A": resid(Ar)},
+                "ours_max_rel_err_vs_reference_output": {
+                    "L": float(torch.linalg.matrix_norm(lo - lr) / torch.linalg.matrix_norm(lr))},
+                "calls": "cusolverDnSpotrf(LOWER) with its workspace sized once (CholeskyFactoriser)"}
+            out["vs_reference_library"] = rms / ms
+        except Exception as exc:
+            out["reference_library"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
+    return out
+
+
+def run_ours_large(args, dev, st, L, rank, world, dist):
+    """The one-matrix Cholesky as a line of its own (for profile captures)."""
+    r = run_chol_large(args, dev, st, L)
+    return {"metric": "matrices/s, one large SPD matrix (CholeskyFactoriser<float>::factorise)", "value": r["value"],
+            "unit": "matrices/s", "n_gpus": world, "steps": max(3, min(args.steps, 5)), "warmup": 2,
+            "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": r["config"], "max_rel_err_vs_fp64": r["max_rel_err_vs_fp64"],
+            "gpu_launches": r["gpu_launches"], "reference_library": r.get("reference_library"),
+            "tflops": r["tflops"]}
+
+
 def _probe_lib():
     from gputils_gb300 import build
 
@@ -1299,9 +1387,11 @@ def main(argv=None):
     L = _lib.lib()
     st = torch.cuda.current_stream().cuda_stream
     fp32_peak()
-    runners = {"d1": run_ours_d1, "d2": run_ours_d2, "d3": run_ours_d3, "d4": run_ours_svd, "d5": run_ours_d5}
+    runners = {"d1": run_ours_d1, "d2": run_ours_d2, "d3": run_ours_d3, "d4": run_ours_svd, "d5": run_ours_d5,
+               "large": run_ours_large}
     line = runners[args.workload](args, dev, st, L, rank, world, dist)
-    cpu = None if args.no_cpu_baseline or rank != 0 else CPU_BASELINES[args.workload](args.cpu_seconds, args)
+    cpu = None if args.no_cpu_baseline or rank != 0 or args.workload == "large" else \
+        CPU_BASELINES[args.workload](args.cpu_seconds, args)
     line["cpu_baseline"] = cpu
     line["fp32_peak"] = dict(FP32_PEAK)
     if args.workload == "d2" and not args.no_workloads:
@@ -1316,6 +1406,7 @@ def main(argv=None):
                 CPU_BASELINES[sub.workload](sub.cpu_seconds, sub)
             subs[name] = workload_summary(r)
             torch.cuda.empty_cache()
+        subs["chol_large_f32"] = run_chol_large(args, dev, st, L)
         line["workloads"] = subs
     if rank == 0:
         print(json.dumps(line), flush=True)
