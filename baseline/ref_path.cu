@@ -15,6 +15,7 @@
 //   refp_spotrf         CholeskyFactoriser<float>: workspace sized once
 //                       (cusolverDnSpotrf_bufferSize), factorise = cusolverDnSpotrf(LOWER)
 //                                                                            tensor.cuh:1703-1709, 1735-1740, 1754-1761
+//   refp_spotrs         CholeskyFactoriser<float>::solve: cusolverDnSpotrs   tensor.cuh:1775-1783
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
@@ -63,6 +64,11 @@ REFP_API int refp_spotrf_bufsize(int n, int *lwork) {
 
 REFP_API int refp_spotrf(int n, float *A, float *work, int lwork, int *info) {
     return (int)cusolverDnSpotrf(g_solver, CUBLAS_FILL_MODE_LOWER, n, A, n, work, lwork, info);
+}
+
+// CholeskyFactoriser<float>::solve: cusolverDnSpotrs(LOWER, nrhs = 1)      tensor.cuh:1775-1783
+REFP_API int refp_spotrs(int n, const float *A, float *B, int *info) {
+    return (int)cusolverDnSpotrs(g_solver, CUBLAS_FILL_MODE_LOWER, n, 1, A, n, B, n, info);
 }
 
 REFP_API int refp_dpotrf_batched(int n, double **A, int *info, int batch) {

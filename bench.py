@@ -408,6 +408,7 @@ class RefLib:
         self.L.refp_sgesvd_loop.argtypes = [ip, ip, vp, vp, vp, vp, vp, ip, vp, ip, ip]
         self.L.refp_spotrf_bufsize.argtypes = [ip, vp]
         self.L.refp_spotrf.argtypes = [ip, vp, vp, ip, vp]
+        self.L.refp_spotrs.argtypes = [ip, vp, vp, vp]
         assert self.L.refp_init(stream) == 0
 
 
@@ -1259,6 +1260,27 @@ def run_chol_large(args, dev, st, L):
 
     ms, A = timed(lambda A: _lib_check(L.gbla_spotrf_large(n, A.data_ptr(), n, info.data_ptr(), ws.data_ptr(),
                                                            ws.numel(), st), "spotrf_large"))
+    def solve_ms(call, Lf):
+        """Median time of one solve with one right-hand side (b ~ N(0,1)), and its solution."""
+        b0 = torch.randn(n, device=dev, generator=g)
+        b = b0.clone()
+        ts = []
+        for rep in range(2 + reps):
+            b.copy_(b0)
+            torch.cuda.synchronize()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record()
+            call(Lf, b)
+            e[1].record()
+            torch.cuda.synchronize()
+            if rep >= 2:
+                ts.append(e[0].elapsed_time(e[1]))
+        return float(np.median(ts)), b0, b
+
+    def solve_err(b0, x):
+        r = A64 @ x.double() - b0.double()
+        return float(torch.linalg.vector_norm(r) / torch.linalg.vector_norm(b0.double()))
+
     out = {"config": {"workload": f"CholeskyFactoriser<float>::factorise, one {n}x{n} SPD matrix (G^T G / n + 0.5 I)",
                       "n": n},
            "value": 1e3 / ms, "unit": "matrices/s", "ms": ms, "tflops": n ** 3 / 3 / ms / 1e9,
@@ -1268,6 +1290,10 @@ def run_chol_large(args, dev, st, L):
            "gpu_launches": (n + 127) // 128 + 2 * ((n + 127) // 128 - 1) + max(0, -(-(n - 256) // 128)),
            "kernels": "k_potrf_diag + k_trsm_panel + k_gemm_bf16_tn (tcgen05, two per panel: next panel's columns "
                       "and the rest, look-ahead on a side stream)"}
+    sms, sb0, sx = solve_ms(lambda Lf, b: _lib_check(L.gbla_spotrs_large(n, 1, Lf.data_ptr(), n, b.data_ptr(), n, st),
+                                                     "spotrs_large"), A)
+    out["solve"] = {"ms": sms, "what": "CholeskyFactoriser<float>::solve, one right-hand side (gbla_spotrs_large)",
+                    "residual": solve_err(sb0, sx)}
     if not args.no_reference_library:
         try:
             R = RefLib(st)
@@ -1285,6 +1311,10 @@ def run_chol_large(args, dev, st, L):
                     "L": float(torch.linalg.matrix_norm(lo - lr) / torch.linalg.matrix_norm(lr))},
                 "calls": "cusolverDnSpotrf(LOWER) with its workspace sized once (CholeskyFactoriser)"}
             out["vs_reference_library"] = rms / ms
+            rsms, rb0, rx = solve_ms(lambda Lf, b: R.L.refp_spotrs(n, C.c_void_p(Lf.data_ptr()), C.c_void_p(b.data_ptr()),
+                                                                   C.c_void_p(rinfo.data_ptr())), Ar)
+            out["reference_library"]["solve"] = {"ms": rsms, "residual": solve_err(rb0, rx),
+                                                 "calls": "cusolverDnSpotrs(LOWER, nrhs = 1)"}
         except Exception as exc:
             out["reference_library"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     return out
@@ -1298,7 +1328,7 @@ def run_ours_large(args, dev, st, L, rank, world, dist):
             "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "config": r["config"], "max_rel_err_vs_fp64": r["max_rel_err_vs_fp64"],
             "gpu_launches": r["gpu_launches"], "reference_library": r.get("reference_library"),
-            "tflops": r["tflops"]}
+            "tflops": r["tflops"], "solve": r.get("solve")}
 
 
 def _probe_lib():

@@ -210,6 +210,151 @@ __global__ void __launch_bounds__(CL_THREADS, 2)
     }
 }
 
+// ------------------------------------------------------------ blocked solve
+// L L^T X = B for one large factor (column stride lda) and nrhs columns of B
+// (column stride ldb), in 128-row blocks: forward, the diagonal block solves
+// its rows (one CTA, a warp per right-hand side) and then every row below
+// subtracts the block's contribution (many CTAs, a thread per row, reading
+// rows of the column block: coalesced); backward, the transposed diagonal
+// block solves and then every row above subtracts its contribution (a
+// thread per row i, reading L(k0 .. k0 + w, i), a contiguous piece of
+// column i).  No workspace; each element of X is written by one thread.
+constexpr int CS_WARPS = 4;     // right-hand sides per CTA of the diagonal solves
+constexpr int CS_THREADS = 128; // rows per CTA of the updates
+
+// Diagonal block of rows [k0, k0 + w): forward (L_kk y = b) or backward
+// (L_kk^T x = y), in place in B.
+template <bool FORWARD>
+__global__ void __launch_bounds__(32 * CS_WARPS)
+    k_trsv_diag(const float *__restrict__ L, int64_t lda, float *__restrict__ B, int64_t ldb, int k0, int w,
+                int nrhs) {
+    extern __shared__ float lb[];  // CL_NB x CL_LD: L_kk, column-major (lower triangle)
+    __shared__ float xs[CS_WARPS][CL_NB];
+    __shared__ float dinv[CL_NB];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const float *lk = L + k0 + (int64_t)k0 * lda;
+    for (int j = warp; j < w; j += CS_WARPS)
+        for (int i = j + lane; i < w; i += 32) lb[j * CL_LD + i] = lk[(int64_t)j * lda + i];
+    __syncthreads();
+    for (int i = tid; i < w; i += 32 * CS_WARPS) dinv[i] = 1.f / lb[i * CL_LD + i];
+    __syncthreads();
+    const int c = blockIdx.x * CS_WARPS + warp;
+    if (c >= nrhs) return;  // whole warp; no block barriers below
+    float *x = xs[warp];
+    float *bc = B + (int64_t)c * ldb + k0;
+    for (int i = lane; i < w; i += 32) x[i] = bc[i];
+    __syncwarp();
+    if (FORWARD) {
+        for (int j = 0; j < w; j++) {
+            const float xj = x[j] * dinv[j];
+            for (int i = j + 1 + lane; i < w; i += 32) x[i] = fmaf(-lb[j * CL_LD + i], xj, x[i]);
+            __syncwarp();
+            if (lane == 0) x[j] = xj;
+            __syncwarp();
+        }
+    } else {
+        for (int j = w - 1; j >= 0; j--) {
+            const float xj = x[j] * dinv[j];
+            for (int i = lane; i < j; i += 32) x[i] = fmaf(-lb[i * CL_LD + j], xj, x[i]);  // L(j, i)
+            __syncwarp();
+            if (lane == 0) x[j] = xj;
+            __syncwarp();
+        }
+    }
+    for (int i = lane; i < w; i += 32) bc[i] = x[i];
+}
+
+// Forward: rows i in [r0, n) lose L(i, k0 .. k0 + w) . y(k0 .. k0 + w).
+__global__ void __launch_bounds__(CS_THREADS)
+    k_trsv_fwd_update(const float *__restrict__ L, int64_t lda, float *__restrict__ B, int64_t ldb, int k0, int w,
+                      int r0, int n, int nrhs) {
+    __shared__ float ys[CL_NB];
+    const int i = r0 + blockIdx.x * CS_THREADS + threadIdx.x;
+    for (int c = 0; c < nrhs; c++) {
+        __syncthreads();
+        for (int j = threadIdx.x; j < w; j += CS_THREADS) ys[j] = B[(int64_t)c * ldb + k0 + j];
+        __syncthreads();
+        if (i < n) {
+            const float *li = L + i + (int64_t)k0 * lda;
+            float s0 = 0.f, s1 = 0.f;
+            int j = 0;
+            for (; j + 1 < w; j += 2) {
+                s0 = fmaf(li[(int64_t)j * lda], ys[j], s0);
+                s1 = fmaf(li[(int64_t)(j + 1) * lda], ys[j + 1], s1);
+            }
+            if (j < w) s0 = fmaf(li[(int64_t)j * lda], ys[j], s0);
+            B[(int64_t)c * ldb + i] -= s0 + s1;
+        }
+    }
+}
+
+// Backward: rows i in [0, k0) lose L(k0 .. k0 + w, i) . x(k0 .. k0 + w).
+__global__ void __launch_bounds__(CS_THREADS)
+    k_trsv_bwd_update(const float *__restrict__ L, int64_t lda, float *__restrict__ B, int64_t ldb, int k0, int w,
+                      int nrhs) {
+    __shared__ float xs[CL_NB];
+    const int i = blockIdx.x * CS_THREADS + threadIdx.x;
+    for (int c = 0; c < nrhs; c++) {
+        __syncthreads();
+        for (int j = threadIdx.x; j < w; j += CS_THREADS) xs[j] = B[(int64_t)c * ldb + k0 + j];
+        __syncthreads();
+        if (i < k0) {
+            const float *li = L + k0 + (int64_t)i * lda;  // column i from row k0: contiguous
+            float s0 = 0.f, s1 = 0.f;
+            int j = 0;
+            for (; j + 1 < w; j += 2) {
+                s0 = fmaf(li[j], xs[j], s0);
+                s1 = fmaf(li[j + 1], xs[j + 1], s1);
+            }
+            if (j < w) s0 = fmaf(li[j], xs[j], s0);
+            B[(int64_t)c * ldb + i] -= s0 + s1;
+        }
+    }
+}
+
+static gbla_status potrs_large(int n, int nrhs, const float *L, int64_t lda, float *B, int64_t ldb, cudaStream_t st) {
+    if (n < 0 || nrhs < 0 || lda < n || ldb < n || (n > 0 && nrhs > 0 && (!L || !B))) return GBLA_INVALID_VALUE;
+    if (n == 0 || nrhs == 0) return GBLA_SUCCESS;
+    const unsigned gd = (unsigned)((nrhs + CS_WARPS - 1) / CS_WARPS);
+    const size_t smem = sizeof(float) * (size_t)CL_NB * CL_LD;
+    static bool attr_done[64] = {false};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(k_trsv_diag<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_trsv_diag<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return from_cuda(e);
+        if (dev >= 0 && dev < 64) attr_done[dev] = true;
+    }
+    for (int k0 = 0; k0 < n; k0 += CL_NB) {
+        const int w = n - k0 < CL_NB ? n - k0 : CL_NB;
+        k_trsv_diag<true><<<gd, 32 * CS_WARPS, smem, st>>>(L, lda, B, ldb, k0, w, nrhs);
+        gbla_status s = launch_status();
+        if (s != GBLA_SUCCESS) return s;
+        const int r0 = k0 + w;
+        if (r0 < n) {
+            k_trsv_fwd_update<<<(unsigned)((n - r0 + CS_THREADS - 1) / CS_THREADS), CS_THREADS, 0, st>>>(
+                L, lda, B, ldb, k0, w, r0, n, nrhs);
+            s = launch_status();
+            if (s != GBLA_SUCCESS) return s;
+        }
+    }
+    for (int k0 = (n - 1) / CL_NB * CL_NB; k0 >= 0; k0 -= CL_NB) {
+        const int w = n - k0 < CL_NB ? n - k0 : CL_NB;
+        k_trsv_diag<false><<<gd, 32 * CS_WARPS, smem, st>>>(L, lda, B, ldb, k0, w, nrhs);
+        gbla_status s = launch_status();
+        if (s != GBLA_SUCCESS) return s;
+        if (k0 > 0) {
+            k_trsv_bwd_update<<<(unsigned)((k0 + CS_THREADS - 1) / CS_THREADS), CS_THREADS, 0, st>>>(L, lda, B, ldb,
+                                                                                                  k0, w, nrhs);
+            s = launch_status();
+            if (s != GBLA_SUCCESS) return s;
+        }
+    }
+    return GBLA_SUCCESS;
+}
+
 // ---------------------------------------------------------------------- host
 // Two sets of BF16 operands (panels alternate), each n x CL_K for SA and SB.
 static size_t potrf_large_ws_bytes(int n) {
@@ -336,6 +481,11 @@ static gbla_status potrf_large(int n, float *A, int64_t lda, int *info, void *ws
 using namespace gbla;
 
 GBLA_API size_t gbla_spotrf_large_workspace_bytes(int n) { return potrf_large_ws_bytes(n); }
+
+GBLA_API gbla_status gbla_spotrs_large(int n, int nrhs, const float *L, int64_t lda, float *B, int64_t ldb,
+                                       cudaStream_t st) {
+    return potrs_large(n, nrhs, L, lda, B, ldb, st);
+}
 
 GBLA_API gbla_status gbla_spotrf_large(int n, float *A, int64_t lda, int *info, void *workspace,
                                        size_t workspace_bytes, cudaStream_t st) {

@@ -95,13 +95,27 @@ gbla_status gbla_dpotrf_batched(int n, double *A, int64_t strideA, int *info, in
  * tensor cores (tcgen05; L21 split exactly into three BF16 parts, the six
  * largest of the nine products accumulated in FP32).  The strictly upper
  * triangle is not touched; *info as gbla_spotrf_batched (set to 0 first).
- * Any n >= 0; the workspace (gbla_spotrf_large_workspace_bytes, 3 KB per
- * row, none for n <= 128) holds the BF16 operands.  Replaces cusolverDnSpotrf
+ * Any n >= 0; the workspace (gbla_spotrf_large_workspace_bytes, 6 KB per
+ * row, none for n <= 128) holds two sets of the BF16 operands (the update of
+ * the rest of the matrix runs on a side stream, overlapping the next panel;
+ * the side stream and its events are made on a thread's first call on a
+ * device, so make that call before capturing a CUDA graph).  Replaces cusolverDnSpotrf
  * (include/tensor.cuh:1742-1761: CholeskyFactoriser::factorise) for the sizes
  * where gbla_spotrf_batched with batch = 1 would leave all but one SM idle. */
 size_t gbla_spotrf_large_workspace_bytes(int n);
 gbla_status gbla_spotrf_large(int n, float *A, int64_t lda, int *info, void *workspace,
                               size_t workspace_bytes, cudaStream_t stream);
+
+/* Solve L L^T X = B in place for ONE large FP32 lower factor L (column stride
+ * lda >= n) and nrhs columns of B (column stride ldb >= n), in 128-row
+ * blocks: each diagonal block solved by one thread block (a warp per
+ * right-hand side), the rows below it (forward) or above it (backward)
+ * updated by n / 128 thread blocks, a thread per row.  No workspace.
+ * Replaces cusolverDnSpotrs (include/tensor.cuh:1775-1783:
+ * CholeskyFactoriser<float>::solve) for the sizes where gbla_spotrs_batched
+ * with batch = 1 runs on one thread block. */
+gbla_status gbla_spotrs_large(int n, int nrhs, const float *L, int64_t lda, float *B, int64_t ldb,
+                              cudaStream_t stream);
 
 /* Solve L_i L_i^T X_i = B_i in place (B_i is n x nrhs) with the lower factor
  * in L_i.  Replaces cusolverDn<t>potrsBatched (include/tensor.cuh:2161-2197)

@@ -27,8 +27,8 @@
  *  - Givens bounds are checked on every index, as the reference documents.
  *  - CholeskyFactoriser<float> above n = 128 runs a blocked factorisation on
  *    the whole GPU (trailing updates on the tensor cores, BF16x3 split with
- *    FP32 accumulation); its workspace is sized and owned by the factoriser
- *    as the reference's cuSOLVER workspace is.
+ *    FP32 accumulation) and a blocked solve; the factorisation's workspace is
+ *    sized and owned by the factoriser as the reference's cuSOLVER workspace is.
  *  - Extensions with no reference counterpart: batched Givens rotations
  *    (DTensor::applyLeft/RightGivensRotationBatched, GivensAnnihilatorBatched),
  *    which rotate every matrix of a tensor in one launch.
@@ -287,6 +287,13 @@ inline gbla_status potrf_one(int n, float *A, int *info, void *ws, size_t ws_byt
 }
 inline gbla_status potrf_one(int n, double *A, int *info, void *, size_t, cudaStream_t st) {
     return gbla_dpotrf_batched(n, A, (int64_t)n * n, info, 1, st);
+}
+inline gbla_status potrs_one(int n, int nrhs, const float *L, float *B, cudaStream_t st) {
+    if (n > 128) return gbla_spotrs_large(n, nrhs, L, n, B, n, st);
+    return gbla_spotrs_batched(n, nrhs, L, (int64_t)n * n, B, (int64_t)n * nrhs, 1, st);
+}
+inline gbla_status potrs_one(int n, int nrhs, const double *L, double *B, cudaStream_t st) {
+    return gbla_dpotrs_batched(n, nrhs, L, (int64_t)n * n, B, (int64_t)n * nrhs, 1, st);
 }
 inline gbla_status potrs(int n, int nrhs, const float *L, float *B, int batch, cudaStream_t st) {
     return gbla_spotrs_batched(n, nrhs, L, (int64_t)n * n, B, (int64_t)n * nrhs, batch, st);
@@ -981,8 +988,8 @@ public:
     void solve(DTensor<T> &b) {
         size_t n = m_matrix->numRows();
         if (b.numRows() != n) throw std::invalid_argument("[Cholesky] A and b incompatible");
-        gputils_detail::check(gputils_detail::potrs((int)n, (int)(b.numCols() * b.numMats()), m_matrix->raw(), b.raw(),
-                                                    1, Session::getInstance().stream(m_matrix->streamIdx())),
+        gputils_detail::check(gputils_detail::potrs_one((int)n, (int)(b.numCols() * b.numMats()), m_matrix->raw(),
+                                                        b.raw(), Session::getInstance().stream(m_matrix->streamIdx())),
                               "Cholesky solve");
     }
 };

@@ -129,3 +129,42 @@ def test_large_potrf_repeat_and_graph_replay(gbla_lib, cuda):
         torch.cuda.synchronize()
         assert torch.equal(A, outs[0])
         assert int(info.item()) == 0
+
+
+@pytest.mark.parametrize("n,nrhs", [(129, 1), (300, 3), (640, 1), (1000, 5), (1536, 2)])
+def test_large_potrs_vs_oracle(gbla_lib, cuda, n, nrhs):
+    """gbla_spotrs_large (blocked solve with one factor, the drop-in
+    CholeskyFactoriser<float>::solve above n = 128) against the FP64 oracle,
+    with the factor from gbla_spotrf_large, and against the single-block
+    gbla_spotrs_batched on the same factor."""
+    import torch
+
+    rng = np.random.default_rng(3 * n + nrhs)
+    A = spd_batch(rng, 1, n, shift=0.5)[0]
+    L, info = _factor_large(gbla_lib, A)
+    assert info == 0
+    b = rng.standard_normal((n, nrhs))
+    Ld = torch.from_numpy(L.T.copy()).cuda()  # column-major
+    ldb = n + 3
+    Bbuf = np.full((nrhs, ldb), np.float32(-2.25), dtype=np.float32)
+    Bbuf[:, :n] = b.T.astype(np.float32)
+    Bd = torch.from_numpy(Bbuf).cuda()
+    assert gbla_lib.gbla_spotrs_large(n, nrhs, ptr(Ld), n, ptr(Bd), ldb, stream()) == 0
+    out = Bd.cpu().numpy()
+    assert np.all(out[:, n:] == np.float32(-2.25))  # rows beyond n untouched
+    x = out[:, :n].T.astype(np.float64)
+    _, xo, _ = O.posv(A[None], b[None])
+    kappa = np.linalg.cond(A)
+    assert rel_err(x[None], xo) < 2e-6 * kappa * np.sqrt(n)
+    # the single-block path on the same factor
+    B1 = torch.from_numpy(np.ascontiguousarray(b.T.astype(np.float32))).cuda()
+    assert gbla_lib.gbla_spotrs_batched(n, nrhs, ptr(Ld), n * n, ptr(B1), n * nrhs, 1, stream()) == 0
+    x1 = B1.cpu().numpy().T.astype(np.float64)
+    assert rel_err(x[None], x1[None]) < 2e-6 * kappa * np.sqrt(n)
+
+
+def test_large_potrs_bad_arguments(gbla_lib, cuda):
+    assert gbla_lib.gbla_spotrs_large(300, 1, None, 299, None, 300, stream()) == 1  # lda < n
+    assert gbla_lib.gbla_spotrs_large(300, 1, None, 300, None, 299, stream()) == 1  # ldb < n
+    assert gbla_lib.gbla_spotrs_large(0, 1, None, 1, None, 1, stream()) == 0
+    assert gbla_lib.gbla_spotrs_large(300, 0, None, 300, None, 300, stream()) == 0
