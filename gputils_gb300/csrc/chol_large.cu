@@ -233,8 +233,13 @@ __global__ void __launch_bounds__(32 * CS_WARPS)
     __shared__ float dinv[CL_NB];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const float *lk = L + k0 + (int64_t)k0 * lda;
-    for (int j = warp; j < w; j += CS_WARPS)
-        for (int i = j + lane; i < w; i += 32) lb[j * CL_LD + i] = lk[(int64_t)j * lda + i];
+    // the w x w block, 16 loads in flight a thread (the strict upper triangle
+    // is loaded but not read)
+#pragma unroll 16
+    for (int e = tid; e < w * w; e += 32 * CS_WARPS) {
+        const int j = e / w, i = e - j * w;
+        lb[j * CL_LD + i] = lk[(int64_t)j * lda + i];
+    }
     __syncthreads();
     for (int i = tid; i < w; i += 32 * CS_WARPS) dinv[i] = 1.f / lb[i * CL_LD + i];
     __syncthreads();
@@ -276,14 +281,10 @@ __global__ void __launch_bounds__(CS_THREADS)
         __syncthreads();
         if (i < n) {
             const float *li = L + i + (int64_t)k0 * lda;
-            float s0 = 0.f, s1 = 0.f;
-            int j = 0;
-            for (; j + 1 < w; j += 2) {
-                s0 = fmaf(li[(int64_t)j * lda], ys[j], s0);
-                s1 = fmaf(li[(int64_t)(j + 1) * lda], ys[j + 1], s1);
-            }
-            if (j < w) s0 = fmaf(li[(int64_t)j * lda], ys[j], s0);
-            B[(int64_t)c * ldb + i] -= s0 + s1;
+            float sp[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 16
+            for (int j = 0; j < w; j++) sp[j & 3] = fmaf(li[(int64_t)j * lda], ys[j], sp[j & 3]);
+            B[(int64_t)c * ldb + i] -= (sp[0] + sp[1]) + (sp[2] + sp[3]);
         }
     }
 }
@@ -300,14 +301,10 @@ __global__ void __launch_bounds__(CS_THREADS)
         __syncthreads();
         if (i < k0) {
             const float *li = L + k0 + (int64_t)i * lda;  // column i from row k0: contiguous
-            float s0 = 0.f, s1 = 0.f;
-            int j = 0;
-            for (; j + 1 < w; j += 2) {
-                s0 = fmaf(li[j], xs[j], s0);
-                s1 = fmaf(li[j + 1], xs[j + 1], s1);
-            }
-            if (j < w) s0 = fmaf(li[j], xs[j], s0);
-            B[(int64_t)c * ldb + i] -= s0 + s1;
+            float sp[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 16
+            for (int j = 0; j < w; j++) sp[j & 3] = fmaf(li[j], xs[j], sp[j & 3]);
+            B[(int64_t)c * ldb + i] -= (sp[0] + sp[1]) + (sp[2] + sp[3]);
         }
     }
 }
