@@ -78,3 +78,24 @@ def test_empty_problems_are_noops(gbla_lib):
 def test_argtypes_come_from_header(gbla_lib, name):
     f = getattr(gbla_lib, name)
     assert f.restype is C.c_int and len(f.argtypes) >= 5
+
+
+def test_large_cholesky_entry_points_validate_host_side(gbla_lib):
+    """gbla_spotrf_large / gbla_spotrs_large reject bad sizes, strides and
+    workspaces before touching the device; empty problems are no-ops."""
+    L = gbla_lib
+    fake = C.c_void_p(0x1000)
+    assert L.gbla_spotrf_large(-1, fake, 1, None, None, 0, None) == INVALID
+    assert L.gbla_spotrf_large(300, fake, 299, None, None, 0, None) == INVALID     # lda < n
+    assert L.gbla_spotrf_large(300, None, 300, None, None, 0, None) == INVALID     # no matrix
+    assert L.gbla_spotrf_large(300, fake, 300, None, fake, 1024, None) == 4        # workspace too small
+    assert L.gbla_spotrf_large(300, fake, 300, None, None, 1 << 30, None) == 4     # no workspace
+    assert L.gbla_spotrf_large(0, None, 1, None, None, 0, None) == 0
+    assert L.gbla_spotrf_large_workspace_bytes(128) == 0
+    assert L.gbla_spotrf_large_workspace_bytes(129) >= 2 * 2 * 129 * 768 * 2       # two sets of two operands
+    assert L.gbla_spotrs_large(-1, 1, fake, 1, fake, 1, None) == INVALID
+    assert L.gbla_spotrs_large(300, 1, fake, 299, fake, 300, None) == INVALID       # lda < n
+    assert L.gbla_spotrs_large(300, 1, fake, 300, fake, 299, None) == INVALID       # ldb < n
+    assert L.gbla_spotrs_large(300, 1, None, 300, fake, 300, None) == INVALID
+    assert L.gbla_spotrs_large(0, 3, None, 1, None, 1, None) == 0
+    assert L.gbla_spotrs_large(300, 0, None, 300, None, 300, None) == 0

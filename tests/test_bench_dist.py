@@ -80,3 +80,19 @@ def test_reference_arm_prints_on_rank0_only():
         assert p.exitcode == 0
     assert '"impl": "reference"' in out[0]
     assert out[1].strip() == ""
+
+
+def test_reference_arm_without_cpu_sample_says_unavailable():
+    """The one-matrix Cholesky has no CPU sample: its reference is the cuSOLVER
+    call on the GPU, reported in our own line."""
+    import contextlib
+    import io
+    import json
+
+    import bench
+
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        bench.main(["--impl", "reference", "--workload", "large", "--steps", "1", "--warmup", "0"])
+    line = json.loads(buf.getvalue().strip().splitlines()[-1])
+    assert line["impl"] == "reference" and "unavailable" in line
