@@ -23,8 +23,13 @@
 //      steps 1 and 2 (look-ahead).
 // The strict upper triangle of A is never written.
 //
-// Replaces cusolverDnSpotrf for one matrix (the reference's CholeskyFactoriser,
-// include/tensor.cuh:1742-1761).
+// The solve with one such factor (gbla_spotrs_large) is blocked the same
+// way: per 128-row block a one-CTA triangular solve and a many-CTA update of
+// the remaining rows (below it forward, above it backward).
+//
+// Replaces cusolverDnSpotrf and cusolverDnSpotrs for one matrix (the
+// reference's CholeskyFactoriser: workspace include/tensor.cuh:1703-1709,
+// factorise :1754-1761, solve :1775-1783).
 #include <cuda_bf16.h>
 #include "common.cuh"
 #include "gemm_bf16.cuh"
